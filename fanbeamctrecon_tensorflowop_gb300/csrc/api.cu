@@ -1,0 +1,359 @@
+// The C ABI (include/ctgb.h): argument validation, plans, workspace, dispatch.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "common.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
+
+ct_status cuda_status(cudaError_t e, const char *where) {
+    if (e == cudaSuccess) return CT_OK;
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), "%s: %s (%d)", where, cudaGetErrorString(e), (int)e);
+    g_last_error = buf;
+    return e == cudaErrorMemoryAllocation ? CT_ERR_ALLOC : CT_ERR_CUDA;
+}
+
+ct_status launch_status(int e, const char *where) { return cuda_status((cudaError_t)e, where); }
+
+// Makes the plan's device current for the duration of a call and restores
+// the caller's device afterwards.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int dev) {
+        err = cudaGetDevice(&prev);
+        if (err == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// Caller-provided scratch, or a stream-ordered allocation released after the
+// last kernel that uses it.
+struct Workspace {
+    void *ptr = nullptr;
+    bool owned = false;
+    cudaStream_t stream = nullptr;
+    ~Workspace() {
+        if (owned && ptr) cudaFreeAsync(ptr, stream);
+    }
+};
+
+ct_status acquire(Workspace &w, void *given, size_t given_bytes, size_t need, cudaStream_t s) {
+    w.stream = s;
+    if (need == 0) return CT_OK;
+    if (given) {
+        if (given_bytes < need) {
+            g_last_error = "workspace smaller than ct_workspace_size";
+            return CT_ERR_WORKSPACE;
+        }
+        w.ptr = given;
+        return CT_OK;
+    }
+    cudaError_t e = cudaMallocAsync(&w.ptr, need, s);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMallocAsync(workspace)");
+    w.owned = true;
+    return CT_OK;
+}
+
+size_t sino_bytes(const ct_plan *p, int batch) {
+    return sizeof(float) * (size_t)batch * p->g.n_views * p->g.n_cols;
+}
+
+ct_status check_call(const ct_plan *p, const void *in, const void *out, int batch) {
+    if (!p) return CT_ERR_NULL_POINTER;
+    if (batch < 0) return CT_ERR_INVALID_ARGUMENT;
+    if (batch > 0 && (!in || !out)) return CT_ERR_NULL_POINTER;
+    if (in && out && in == out) return CT_ERR_INVALID_ARGUMENT;
+    return CT_OK;
+}
+
+size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
+    switch (op) {
+        case CT_OP_FBP:
+        case CT_OP_FBP_ADJOINT:
+        case CT_OP_FDK_BP:
+            return sino_bytes(p, batch);
+        default:
+            return 0;
+    }
+}
+
+void free_plan(ct_plan *p) {
+    if (!p) return;
+    cudaFree(p->d_view_cs);
+    cudaFree(p->d_ray);
+    cudaFree(p->d_nsamp);
+    cudaFree(p->d_taps);
+    delete p;
+}
+
+template <typename T>
+ct_status upload(T **dst, const std::vector<T> &src) {
+    *dst = nullptr;
+    if (src.empty()) return CT_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dst), sizeof(T) * src.size());
+    if (e != cudaSuccess) return cuda_status(e, "cudaMalloc(plan table)");
+    e = cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice);
+    return cuda_status(e, "cudaMemcpy(plan table)");
+}
+
+// Filtered backprojection shared by ct_fbp_fan and ct_fdk_bp.
+ct_status filtered_bp(const ct_plan *p, const float *d_sino, float *d_img, int batch,
+                      void *d_work, size_t work_bytes, cudaStream_t s, const char *name) {
+    Workspace w;
+    ct_status st = acquire(w, d_work, work_bytes, sino_bytes(p, batch), s);
+    if (st != CT_OK) return st;
+    float *filt = static_cast<float *>(w.ptr);
+    st = launch_status(ctk::ramp_filter(p, d_sino, filt, batch * p->g.n_views, s), name);
+    if (st != CT_OK) return st;
+    return launch_status(ctk::bp_fan(p, filt, d_img, batch, 1, s), name);
+}
+
+}  // namespace
+
+void ct_count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+extern "C" {
+
+const char *ct_status_string(ct_status s) {
+    switch (s) {
+        case CT_OK: return "CT_OK";
+        case CT_ERR_INVALID_ARGUMENT: return "CT_ERR_INVALID_ARGUMENT: invalid geometry, size or option";
+        case CT_ERR_NULL_POINTER: return "CT_ERR_NULL_POINTER: a required pointer is NULL";
+        case CT_ERR_WORKSPACE: return "CT_ERR_WORKSPACE: workspace smaller than required";
+        case CT_ERR_CUDA: return "CT_ERR_CUDA: a CUDA call failed";
+        case CT_ERR_ALLOC: return "CT_ERR_ALLOC: allocation failed";
+        case CT_ERR_UNSUPPORTED: return "CT_ERR_UNSUPPORTED: not supported by this build";
+        case CT_ERR_TIMEOUT: return "CT_ERR_TIMEOUT: a bounded device wait gave up";
+    }
+    return "unknown ct_status";
+}
+
+const char *ct_version(void) { return "ctgb 0.1.0 (sm_103a)"; }
+
+const char *ct_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t ct_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+ct_status ct_geom_from_param16(const float param[16], ct_fan_geom *out) {
+    return ct_decode_param16(param, out);
+}
+
+ct_status ct_fp_ray_table(const ct_fan_geom *geom, const float *angles, int n_angles,
+                          float *ray4, int32_t *nsamp) {
+    if (!geom || !angles || !ray4 || !nsamp) return CT_ERR_NULL_POINTER;
+    ct_status st = ct_validate_geom(geom);
+    if (st != CT_OK) return st;
+    if (n_angles != geom->n_views) return CT_ERR_INVALID_ARGUMENT;
+    ct_host_tables t;
+    ct_build_ray_table(geom, angles, &t);
+    std::memcpy(ray4, t.ray.data(), sizeof(float) * t.ray.size());
+    std::memcpy(nsamp, t.nsamp.data(), sizeof(int32_t) * t.nsamp.size());
+    return CT_OK;
+}
+
+ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_angles,
+                         const ct_plan_opts *opts, ct_plan **out) {
+    if (!geom || !angles || !out) return CT_ERR_NULL_POINTER;
+    *out = nullptr;
+    ct_status st = ct_validate_geom(geom);
+    if (st != CT_OK) return st;
+    if (n_angles != geom->n_views) return CT_ERR_INVALID_ARGUMENT;
+    for (int v = 0; v < n_angles; ++v)
+        if (!std::isfinite(angles[v])) return CT_ERR_INVALID_ARGUMENT;
+    ct_plan_opts o;
+    std::memset(&o, 0, sizeof(o));
+    if (opts) {
+        o = *opts;
+        for (int r : o.reserved)
+            if (r != 0) return CT_ERR_INVALID_ARGUMENT;
+    }
+    if (o.filter_window != CT_WINDOW_RAMLAK && o.filter_window != CT_WINDOW_SHEPP_LOGAN)
+        return CT_ERR_INVALID_ARGUMENT;
+    if (o.filter_algo < CT_FILTER_AUTO || o.filter_algo > CT_FILTER_TOEPLITZ_TC)
+        return CT_ERR_INVALID_ARGUMENT;
+    if (o.filter_algo == CT_FILTER_TOEPLITZ_TC) return CT_ERR_UNSUPPORTED;
+
+    ct_host_tables t;
+    ct_build_view_table(geom, angles, &t);
+    ct_build_ray_table(geom, angles, &t);
+    ct_build_filter_taps(geom, o.filter_window, &t);
+
+    ct_plan *p = new (std::nothrow) ct_plan();
+    if (!p) return CT_ERR_ALLOC;
+    p->g = *geom;
+    p->opts = o;
+    p->filter_algo = CT_FILTER_DIRECT;
+    p->fp_weight = (float)(CT_FP_STEP * (double)geom->dx);
+    p->fov_r2 = geom->rfov * geom->rfov;
+    p->total_samples = t.total_samples;
+    p->max_nsamp = t.max_nsamp;
+    p->h_view_cs = t.view_cs;
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e != cudaSuccess) {
+        delete p;
+        return cuda_status(e, "cudaGetDevice");
+    }
+    if ((st = upload(&p->d_view_cs, t.view_cs)) != CT_OK ||
+        (st = upload(&p->d_ray, t.ray)) != CT_OK || (st = upload(&p->d_nsamp, t.nsamp)) != CT_OK ||
+        (st = upload(&p->d_taps, t.taps)) != CT_OK) {
+        free_plan(p);
+        return st;
+    }
+    *out = p;
+    return CT_OK;
+}
+
+ct_status ct_plan_destroy(ct_plan *plan) {
+    if (!plan) return CT_OK;
+    DeviceScope ds(plan->device);
+    free_plan(plan);
+    return CT_OK;
+}
+
+ct_status ct_plan_geom(const ct_plan *plan, ct_fan_geom *out) {
+    if (!plan || !out) return CT_ERR_NULL_POINTER;
+    *out = plan->g;
+    return CT_OK;
+}
+
+ct_status ct_workspace_size(const ct_plan *plan, ct_op op, int batch, size_t *bytes) {
+    if (!plan || !bytes) return CT_ERR_NULL_POINTER;
+    if (batch < 0 || op < CT_OP_FP || op > CT_OP_BP_ADJOINT) return CT_ERR_INVALID_ARGUMENT;
+    *bytes = op_workspace(plan, op, batch);
+    return CT_OK;
+}
+
+ct_status ct_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                    void *d_work, size_t work_bytes, ct_stream stream) {
+    (void)d_work;
+    (void)work_bytes;
+    ct_status st = check_call(plan, d_img, d_sino, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::fp_fan(plan, d_img, d_sino, batch, stream), "ct_fp_fan");
+}
+
+ct_status ct_fp_fan_adjoint(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                            void *d_work, size_t work_bytes, ct_stream stream) {
+    (void)d_work;
+    (void)work_bytes;
+    ct_status st = check_call(plan, d_sino, d_img, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::fp_fan_adjoint(plan, d_sino, d_img, batch, stream),
+                         "ct_fp_fan_adjoint");
+}
+
+ct_status ct_bp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                    ct_stream stream) {
+    ct_status st = check_call(plan, d_sino, d_img, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::bp_fan(plan, d_sino, d_img, batch, 0, stream), "ct_bp_fan");
+}
+
+ct_status ct_bp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                            ct_stream stream) {
+    ct_status st = check_call(plan, d_img, d_sino, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::bp_fan_transpose(plan, d_img, d_sino, batch, 0, stream),
+                         "ct_bp_fan_adjoint");
+}
+
+ct_status ct_ramp_filter(const ct_plan *plan, const float *d_sino, float *d_out, int rows,
+                         ct_stream stream) {
+    ct_status st = check_call(plan, d_sino, d_out, rows);
+    if (st != CT_OK || rows == 0) return st;
+    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::ramp_filter(plan, d_sino, d_out, rows, stream), "ct_ramp_filter");
+}
+
+ct_status ct_fbp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                     void *d_work, size_t work_bytes, ct_stream stream) {
+    ct_status st = check_call(plan, d_sino, d_img, batch);
+    if (st != CT_OK || batch == 0) return st;
+    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return filtered_bp(plan, d_sino, d_img, batch, d_work, work_bytes, stream, "ct_fbp_fan");
+}
+
+ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                             void *d_work, size_t work_bytes, ct_stream stream) {
+    ct_status st = check_call(plan, d_img, d_sino, batch);
+    if (st != CT_OK || batch == 0) return st;
+    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, sino_bytes(plan, batch), stream);
+    if (st != CT_OK) return st;
+    float *tmp = static_cast<float *>(w.ptr);
+    st = launch_status(ctk::bp_fan_transpose(plan, d_img, tmp, batch, 1, stream),
+                       "ct_fbp_fan_adjoint");
+    if (st != CT_OK) return st;
+    // The row filter is a symmetric Toeplitz matrix: its transpose is itself.
+    return launch_status(ctk::ramp_filter(plan, tmp, d_sino, batch * plan->g.n_views, stream),
+                         "ct_fbp_fan_adjoint");
+}
+
+ct_status ct_fdk_bp(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                    void *d_work, size_t work_bytes, ct_stream stream) {
+    ct_status st = check_call(plan, d_sino, d_img, batch);
+    if (st != CT_OK || batch == 0) return st;
+    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    // nZ = nRows = 1 (FDK/FBP.cc:85,98): the single-row view texture clamps
+    // every row index to row 0, so CB_EA reduces to the weighted fan BP with
+    // detector shift.
+    return filtered_bp(plan, d_sino, d_img, batch, d_work, work_bytes, stream, "ct_fdk_bp");
+}
+
+ct_status ct_plain_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                          ct_stream stream) {
+    ct_status st = check_call(plan, d_img, d_sino, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::plain_fp_fan(plan, d_img, d_sino, batch, stream), "ct_plain_fp_fan");
+}
+
+ct_status ct_plain_fp_fan_adjoint(const ct_plan *plan, const float *d_sino, float *d_img,
+                                  int batch, ct_stream stream) {
+    ct_status st = check_call(plan, d_sino, d_img, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::plain_fp_fan_adjoint(plan, d_sino, d_img, batch, stream),
+                         "ct_plain_fp_fan_adjoint");
+}
+
+ct_status ct_plain_bp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                          ct_stream stream) {
+    ct_status st = check_call(plan, d_sino, d_img, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::plain_bp_fan(plan, d_sino, d_img, batch, stream), "ct_plain_bp_fan");
+}
+
+}  // extern "C"

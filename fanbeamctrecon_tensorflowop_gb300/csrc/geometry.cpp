@@ -1,0 +1,176 @@
+// Host-side geometry: parameter decoding and the FP64-derived per-view and
+// per-ray tables the kernels consume.  Built with -ffp-contract=off so the
+// double-precision tables are identical on x86-64 and aarch64 hosts.
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace {
+bool finite(float v) { return std::isfinite(v); }
+// Truncation toward zero of a float attribute, as int(parameter(k)) does in
+// the reference constructors (FP/transform.cc:61,64-66,75).
+bool to_int(float v, int32_t *out) {
+    if (!finite(v) || v <= -2147483648.0f || v >= 2147483648.0f) return false;
+    *out = static_cast<int32_t>(v);
+    return true;
+}
+}  // namespace
+
+// Mirrors FPFanCurveOp's constructor arithmetic (FP/transform.cc:59-76) and the
+// FDK op's extra fields (FDK/FBP.cc:82-84), in float, term for term.
+ct_status ct_decode_param16(const float p[16], ct_fan_geom *g) {
+    if (!p || !g) return CT_ERR_NULL_POINTER;
+    std::memset(g, 0, sizeof(*g));
+    const float PI = CT_REF_PI;
+    g->sdd = p[0];
+    g->sid = p[1];
+    if (!to_int(p[2], &g->n_views)) return CT_ERR_INVALID_ARGUMENT;
+    g->full_angle = p[3];
+    if (!to_int(p[4], &g->n_cols)) return CT_ERR_INVALID_ARGUMENT;
+    if (!to_int(p[5], &g->nx)) return CT_ERR_INVALID_ARGUMENT;
+    if (!to_int(p[6], &g->ny)) return CT_ERR_INVALID_ARGUMENT;
+    g->rfov = p[7];
+    g->shift = p[9];
+    if (!to_int(p[11], &g->n_slices)) return CT_ERR_INVALID_ARGUMENT;
+    g->det_bottom = p[13];
+    g->drow = p[14];
+    g->dz = p[15];
+    if (g->n_views <= 0 || g->nx <= 0 || g->ny <= 0) return CT_ERR_INVALID_ARGUMENT;
+    // dAngle = dRange/nViews*PI/180.0f (FP/transform.cc:63)
+    float d_angle = g->full_angle / static_cast<float>(g->n_views);
+    d_angle = d_angle * PI;
+    g->d_angle = d_angle / 180.0f;
+    // dx = 2.0f*rFOV/nX; xmin = -0.5f*nX*dx (FP/transform.cc:68-71)
+    float two_r = 2.0f * g->rfov;
+    g->dx = two_r / static_cast<float>(g->nx);
+    g->dy = two_r / static_cast<float>(g->ny);
+    float hx = -0.5f * static_cast<float>(g->nx);
+    float hy = -0.5f * static_cast<float>(g->ny);
+    g->xmin = hx * g->dx;
+    g->ymin = hy * g->dy;
+    // dCol, dLeft, start angle: parameter(k)*PI/180.0f (FP/transform.cc:72-76)
+    float t = p[8] * PI;
+    g->dcol = t / 180.0f;
+    t = p[10] * PI;
+    g->left = t / 180.0f;
+    t = p[12] * PI;
+    g->start_angle = t / 180.0f;
+    return ct_validate_geom(g);
+}
+
+// The reference checks nothing; these are the conditions under which its
+// formulas describe a real fan-beam scan (pixels in front of the source, a
+// non-degenerate detector) and under which 32-bit indexing is safe.
+ct_status ct_validate_geom(const ct_fan_geom *g) {
+    if (!g) return CT_ERR_NULL_POINTER;
+    if (g->n_views <= 0 || g->n_cols <= 0 || g->nx <= 0 || g->ny <= 0)
+        return CT_ERR_INVALID_ARGUMENT;
+    if ((int64_t)g->n_views * g->n_cols >= (int64_t)1 << 31) return CT_ERR_INVALID_ARGUMENT;
+    if ((int64_t)g->nx * g->ny >= (int64_t)1 << 31) return CT_ERR_INVALID_ARGUMENT;
+    if (g->nx > 32768 || g->ny > 32768 || g->n_cols > (1 << 20)) return CT_ERR_INVALID_ARGUMENT;
+    const float vals[] = {g->sdd, g->sid, g->full_angle, g->rfov, g->shift, g->det_bottom,
+                          g->drow,  g->dz,  g->d_angle,    g->dx,   g->dy,    g->xmin,
+                          g->ymin,  g->dcol, g->left};
+    for (float v : vals)
+        if (!finite(v)) return CT_ERR_INVALID_ARGUMENT;
+    if (!(g->rfov > 0.0f) || !(g->sid > g->rfov)) return CT_ERR_INVALID_ARGUMENT;
+    if (!(g->dcol > 0.0f) || !(g->dx > 0.0f) || !(g->dy > 0.0f)) return CT_ERR_INVALID_ARGUMENT;
+    return CT_OK;
+}
+
+// c = -cos(beta), s = -sin(beta): the reference passes -sinf(angle) and
+// -cosf(angle) to every BP kernel (BP/transform.cu:116, FBP/transform.cu:110,
+// FDK/GPURecon_GPU.cu:255).
+void ct_build_view_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t) {
+    const int V = g->n_views;
+    t->view_cs.assign(2 * (size_t)V, 0.0f);
+    for (int v = 0; v < V; ++v) {
+        const double beta = angles[v];
+        t->view_cs[2 * v + 0] = static_cast<float>(-std::cos(beta));
+        t->view_cs[2 * v + 1] = static_cast<float>(-std::sin(beta));
+    }
+}
+
+// Per-ray table of GenerateRayTraceMap_FB_ReconImage_OneView_kernel
+// (FP/transform.cu:64-101), evaluated in double: ray angle
+// beta + left + (i+1/2) dcol, signed distance R/dx * sin(gamma) of the ray from
+// the isocentre, the two intersections of the ray with the FOV circle of
+// radius rfov/dx (pixel units), chord length L, n = floor(L/0.125), start =
+// first intersection + rfov/dx, step = chord/n.  A ray that misses the circle
+// (the reference's sqrtf of a negative number, :81) or touches it (L = 0)
+// gets n = 0 and contributes 0.
+void ct_build_ray_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t) {
+    const int V = g->n_views, C = g->n_cols;
+    const size_t R = (size_t)V * C;
+    t->ray.assign(4 * R, 0.0f);
+    t->nsamp.assign(R, 0);
+    t->max_nsamp = 0;
+    t->total_samples = 0;
+    const double dx = g->dx;
+    const double src_px = (double)g->sid / dx;
+    const double fov_px = (double)g->rfov / dx;
+    const double left = g->left, dcol = g->dcol;
+    for (int v = 0; v < V; ++v) {
+        const double beta = angles[v];
+        for (int i = 0; i < C; ++i) {
+            const size_t r = (size_t)v * C + i;
+            const double gam = left + (i + 0.5) * dcol;
+            const double th = beta + gam;
+            const double sn = std::sin(th), cs = std::cos(th);
+            const double dist = src_px * std::sin(gam);
+            const double h = fov_px * fov_px - dist * dist;
+            if (!(h > 0.0)) continue;
+            const double x1 = -std::sqrt(h), x2 = -x1, y1 = -dist, y2 = -dist;
+            const double ax = x1 * cs - y1 * sn, ay = x1 * sn + y1 * cs;
+            const double bx = x2 * cs - y2 * sn, by = x2 * sn + y2 * cs;
+            const double L = std::sqrt((ax - bx) * (ax - bx) + (ay - by) * (ay - by));
+            const double q = std::floor(L / CT_FP_STEP);
+            if (!(q >= 1.0)) continue;
+            const int32_t n = static_cast<int32_t>(q);
+            t->nsamp[r] = n;
+            t->ray[4 * r + 0] = static_cast<float>(ax + fov_px);
+            t->ray[4 * r + 1] = static_cast<float>(ay + fov_px);
+            t->ray[4 * r + 2] = static_cast<float>((bx - ax) / n);
+            t->ray[4 * r + 3] = static_cast<float>((by - ay) / n);
+            if (n > t->max_nsamp) t->max_nsamp = n;
+            t->total_samples += n;
+        }
+    }
+}
+
+// Ramp filter taps h[n], n in [-(C-1), C-1], stored at index n + C - 1 and
+// multiplied by R * d_angle * dcol (FBP/transform.cu:149-162,
+// FDK/GPURecon_GPU.cu:184-200).  Ram-Lak is Hsieh's equiangular h'' form with
+// the 0.5 redundancy factor: h[0] = 0.5/(4 dcol^2), h[odd n] =
+// -0.5/(pi^2 sin^2(n dcol)), h[even n != 0] = 0.  Shepp-Logan is
+// 0.5 * 2/(pi^2 dcol^2 (1-4n^2)) mapped to the fan by (n dcol/sin(n dcol))^2.
+void ct_build_filter_taps(const ct_fan_geom *g, int window, ct_host_tables *t) {
+    const int C = g->n_cols;
+    t->taps.assign(2 * (size_t)C - 1, 0.0f);
+    const double pi = (double)CT_REF_PI;
+    const double dc = g->dcol;
+    const double scale = (double)g->sid * (double)g->d_angle * dc;
+    for (int n = -(C - 1); n <= C - 1; ++n) {
+        double h;
+        if (window == CT_WINDOW_SHEPP_LOGAN) {
+            if (n == 0) {
+                h = 0.5 * 2.0 / (pi * pi * dc * dc);
+            } else {
+                const double s = std::sin(n * dc);
+                h = 0.5 * 2.0 * (double)n * (double)n /
+                    (pi * pi * s * s * (1.0 - 4.0 * (double)n * (double)n));
+            }
+        } else {
+            if (n == 0) {
+                h = 0.5 / (4.0 * dc * dc);
+            } else if (n % 2 != 0) {
+                const double s = std::sin(n * dc);
+                h = -0.5 / (pi * pi * s * s);
+            } else {
+                h = 0.0;
+            }
+        }
+        t->taps[(size_t)(n + C - 1)] = static_cast<float>(h * scale);
+    }
+}

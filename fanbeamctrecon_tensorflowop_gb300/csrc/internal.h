@@ -1,0 +1,72 @@
+// Internal declarations shared by the ctgb translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/ctgb.h"
+
+// Float literal the reference uses for pi in every op (FP/transform.h:1,
+// GPURecon_GPU.h:3).  Geometry decoding keeps it so decoded values match.
+#define CT_REF_PI 3.14159265359f
+
+// Sample step of the ray-driven projector, in pixels (FP/transform.cu:10).
+#define CT_FP_STEP 0.125
+
+// Host-side (FP64-derived) geometry tables; built without CUDA.
+struct ct_host_tables {
+    // Per view: rotation constants as the reference BP kernels take them,
+    // c = -cos(beta), s = -sin(beta) (BP/transform.cu:116).
+    std::vector<float> view_cs;      // [2*V]
+    // Per ray (view-major, [V][C]): start (x, y) and step (x, y) in texture
+    // pixel coordinates, and the sample count floor(chord/0.125)
+    // (FP/transform.cu:64-101).
+    std::vector<float> ray;          // [4*V*C]
+    std::vector<int32_t> nsamp;      // [V*C]
+    std::vector<float> taps;         // [2C-1] ramp filter taps, index n + C - 1
+    int32_t max_nsamp = 0;
+    double total_samples = 0;        // sum of nsamp over all rays
+};
+
+// geometry.cpp
+ct_status ct_decode_param16(const float p[16], ct_fan_geom *g);
+ct_status ct_validate_geom(const ct_fan_geom *g);
+void ct_build_view_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
+void ct_build_ray_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
+void ct_build_filter_taps(const ct_fan_geom *g, int window, ct_host_tables *t);
+
+struct ct_plan {
+    ct_fan_geom g;
+    ct_plan_opts opts;
+    int device;
+    int filter_algo;                 // resolved ct_filter_algo (never AUTO)
+    float fp_weight;                 // 0.125*dx (FP/transform.cu:144)
+    float fov_r2;                    // rfov^2 (BP/transform.cu:116)
+    double total_samples;
+    int32_t max_nsamp;
+    std::vector<float> h_view_cs;    // host copy of the view table
+    // device copies of ct_host_tables (owned)
+    float *d_view_cs;                // [2V]
+    float *d_ray;                    // [4VC]
+    int32_t *d_nsamp;                // [VC]
+    float *d_taps;                   // [2C-1]
+};
+
+// Kernel launchers (defined in the .cu files).  Each returns the launch error.
+namespace ctk {
+int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *stream);
+int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
+// mode 0: unweighted BP, 1: 1/(U^2+t^2)-weighted (FBP / FDK 2-D)
+int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weighted, void *stream);
+int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch, int weighted,
+                     void *stream);
+int ramp_filter(const ct_plan *p, const float *in, float *out, int rows, void *stream);
+size_t ramp_direct_smem(int C);
+int plain_fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *stream);
+int plain_fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
+int plain_bp_fan(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
+}  // namespace ctk
+
+// Launch accounting (api.cu).
+void ct_count_launch(uint64_t n = 1);

@@ -1,0 +1,203 @@
+"""PyTorch-facing operators over the C ABI.
+
+``FanPlan`` owns a ct_plan (geometry decoded from the reference's 16-float
+parameter vector plus the view angles) on one CUDA device.  Its methods take
+and return float32 CUDA tensors -- images [B, ny, nx], sinograms
+[B, n_views, n_cols] -- and enqueue the library's kernels on the current
+torch stream.  Scratch space comes from torch's caching allocator.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import decode
+
+_plan_cache: dict = {}
+_plan_lock = threading.Lock()
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+class FanPlan:
+    """A fan-beam geometry bound to one CUDA device."""
+
+    def __init__(self, param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK,
+                 filter_algo: int = _lib.FILTER_AUTO):
+        self._lib = _lib.load()
+        self.param16 = np.ascontiguousarray(np.asarray(param16, dtype=np.float32)).copy()
+        self.angles = np.ascontiguousarray(np.asarray(angles, dtype=np.float32)).copy()
+        self.geom = decode(self.param16)
+        self.window = int(window)
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("FanPlan needs a CUDA device")
+        opts = _lib.CtPlanOpts()
+        opts.filter_window = int(window)
+        opts.filter_algo = int(filter_algo)
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            st = self._lib.ct_plan_create(
+                ctypes.byref(self.geom),
+                self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                int(self.angles.shape[0]), ctypes.byref(opts), ctypes.byref(handle))
+        _lib.check(st, "ct_plan_create")
+        self._h = handle
+
+    # -- lifetime ---------------------------------------------------------------
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.ct_plan_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- shapes -----------------------------------------------------------------
+    @property
+    def image_shape(self) -> tuple[int, int]:
+        return (self.geom.ny, self.geom.nx)
+
+    @property
+    def sino_shape(self) -> tuple[int, int]:
+        return (self.geom.n_views, self.geom.n_cols)
+
+    def _stream(self) -> int:
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _check_in(self, t: torch.Tensor, tail: tuple[int, int], what: str) -> torch.Tensor:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{what} must be a torch.Tensor")
+        if t.device != self.device:
+            raise ValueError(f"{what} is on {t.device}, plan is on {self.device}")
+        if t.dtype != torch.float32:
+            raise TypeError(f"{what} must be float32, got {t.dtype}")
+        if t.dim() == 2:
+            t = t.unsqueeze(0)
+        if t.dim() != 3 or tuple(t.shape[1:]) != tail:
+            raise ValueError(f"{what} must be [B, {tail[0]}, {tail[1]}], got {tuple(t.shape)}")
+        return t.contiguous()
+
+    def workspace_bytes(self, op: int, batch: int) -> int:
+        n = ctypes.c_size_t()
+        _lib.check(self._lib.ct_workspace_size(self._h, op, batch, ctypes.byref(n)),
+                   "ct_workspace_size")
+        return int(n.value)
+
+    def _work(self, op: int, batch: int):
+        nbytes = self.workspace_bytes(op, batch)
+        if nbytes == 0:
+            return None, 0
+        return torch.empty(nbytes, dtype=torch.uint8, device=self.device), nbytes
+
+    def _run(self, name: str, op: int | None, x: torch.Tensor, out_tail: tuple[int, int],
+             with_work: bool, out: torch.Tensor | None = None) -> torch.Tensor:
+        B = x.shape[0]
+        if out is None:
+            out = torch.empty((B, *out_tail), dtype=torch.float32, device=self.device)
+        fn = getattr(self._lib, name)
+        with torch.cuda.device(self.device):
+            if with_work:
+                work, nbytes = self._work(op, B)
+                st = fn(self._h, _ptr(x), _ptr(out), B, _ptr(work), nbytes, self._stream())
+            else:
+                st = fn(self._h, _ptr(x), _ptr(out), B, self._stream())
+        _lib.check(st, name)
+        return out
+
+    # -- operators --------------------------------------------------------------
+    def fp(self, img: torch.Tensor, out=None) -> torch.Tensor:
+        """Ray-driven forward projection (FPFanCurve)."""
+        x = self._check_in(img, self.image_shape, "image")
+        return self._run("ct_fp_fan", _lib.OP_FP, x, self.sino_shape, True, out)
+
+    def fp_adjoint(self, sino: torch.Tensor, out=None) -> torch.Tensor:
+        """Exact transpose of ``fp``."""
+        y = self._check_in(sino, self.sino_shape, "sinogram")
+        return self._run("ct_fp_fan_adjoint", _lib.OP_FP_ADJOINT, y, self.image_shape, True, out)
+
+    def bp(self, sino: torch.Tensor, out=None) -> torch.Tensor:
+        """Unweighted pixel-driven backprojection (BPFanCurve)."""
+        y = self._check_in(sino, self.sino_shape, "sinogram")
+        return self._run("ct_bp_fan", None, y, self.image_shape, False, out)
+
+    def bp_adjoint(self, img: torch.Tensor, out=None) -> torch.Tensor:
+        """Exact transpose of ``bp``."""
+        x = self._check_in(img, self.image_shape, "image")
+        return self._run("ct_bp_fan_adjoint", None, x, self.sino_shape, False, out)
+
+    def ramp_filter(self, sino: torch.Tensor, out=None) -> torch.Tensor:
+        """Row ramp filter with the plan's window."""
+        y = self._check_in(sino, self.sino_shape, "sinogram")
+        if out is None:
+            out = torch.empty_like(y)
+        with torch.cuda.device(self.device):
+            st = self._lib.ct_ramp_filter(self._h, _ptr(y), _ptr(out), y.shape[0] * y.shape[1],
+                                          self._stream())
+        _lib.check(st, "ct_ramp_filter")
+        return out
+
+    def fbp(self, sino: torch.Tensor, out=None) -> torch.Tensor:
+        """Filtered backprojection (FBPFanCurve)."""
+        y = self._check_in(sino, self.sino_shape, "sinogram")
+        return self._run("ct_fbp_fan", _lib.OP_FBP, y, self.image_shape, True, out)
+
+    def fbp_adjoint(self, img: torch.Tensor, out=None) -> torch.Tensor:
+        """Exact transpose of ``fbp``."""
+        x = self._check_in(img, self.image_shape, "image")
+        return self._run("ct_fbp_fan_adjoint", _lib.OP_FBP_ADJOINT, x, self.sino_shape, True, out)
+
+    def fdk_bp(self, sino: torch.Tensor, out=None) -> torch.Tensor:
+        """The reference FDK "BackProjection" op (one detector row, one slice)."""
+        y = self._check_in(sino, self.sino_shape, "sinogram")
+        return self._run("ct_fdk_bp", _lib.OP_FDK_BP, y, self.image_shape, True, out)
+
+    # -- the plain per-view launch loop (measurement baseline) -------------------
+    def plain_fp(self, img: torch.Tensor) -> torch.Tensor:
+        x = self._check_in(img, self.image_shape, "image")
+        return self._run("ct_plain_fp_fan", None, x, self.sino_shape, False)
+
+    def plain_fp_adjoint(self, sino: torch.Tensor) -> torch.Tensor:
+        y = self._check_in(sino, self.sino_shape, "sinogram")
+        return self._run("ct_plain_fp_fan_adjoint", None, y, self.image_shape, False)
+
+    def plain_bp(self, sino: torch.Tensor) -> torch.Tensor:
+        y = self._check_in(sino, self.sino_shape, "sinogram")
+        return self._run("ct_plain_bp_fan", None, y, self.image_shape, False)
+
+
+def get_plan(param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK) -> FanPlan:
+    """A cached FanPlan for (parameter, angles, device, window)."""
+    p = np.ascontiguousarray(np.asarray(param16, dtype=np.float32))
+    a = np.ascontiguousarray(np.asarray(angles, dtype=np.float32))
+    if device is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    device = torch.device(device)
+    if device.type == "cuda" and device.index is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    key = (p.tobytes(), a.tobytes(), str(device), int(window))
+    with _plan_lock:
+        plan = _plan_cache.get(key)
+        if plan is None:
+            plan = FanPlan(p, a, device=device, window=window)
+            _plan_cache[key] = plan
+        return plan
+
+
+def clear_plan_cache() -> None:
+    with _plan_lock:
+        for p in _plan_cache.values():
+            p.close()
+        _plan_cache.clear()

@@ -1,0 +1,245 @@
+/*
+ * ctgb.h -- C ABI of the GB300 (sm_103a) fan-beam / cone-beam CT operators.
+ *
+ * This is the drop-in boundary for the four TensorFlow-1 custom ops of
+ * FanBeamCTRecon_TensorflowOp:
+ *
+ *   FPFanCurve      (FP/transform.cc:17-37, kernel FP/transform.cu:64-146)
+ *   BPFanCurve      (BP/transform.cc:17-36, kernel BP/transform.cu:67-95)
+ *   FBPFanCurve     (FBP/transform.cc:17-36, kernel FBP/transform.cu:61-89,
+ *                    host ramp filter FBP/transform.cu:147-178)
+ *   BackProjection  (FDK/FBP.cc:16-35, kernel FDK/GPURecon_GPU.cu:15-50,
+ *                    host ramp filter FDK/GPURecon_GPU.cu:184-217)
+ *
+ * Conventions shared by every entry point:
+ *   - All array pointers prefixed d_ are DEVICE pointers; the caller owns them.
+ *   - Images are float32 [batch][ny][nx] (x fastest), as the reference's
+ *     cudaArray copies read them (FP/transform.cu:222,231; BP/transform.cu:87).
+ *   - Sinograms are float32 [batch][n_views][n_cols] (FP/transform.cu:250).
+ *   - Every operator OVERWRITES its output (the reference FDK op accumulated
+ *     into an unzeroed buffer, FDK/GPURecon_GPU.cu:237-238; this one does not).
+ *   - Work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ *     stream).  Calls return after enqueueing; no device-wide synchronisation.
+ *   - Plans are immutable after creation and may be used concurrently from
+ *     several host threads and streams (the reference kept geometry in
+ *     module-global __constant__ memory, FP/transform.cu:15-62, so two
+ *     differently-configured instances clobbered each other).
+ *   - Errors are returned as ct_status; the library never exits the process
+ *     (the reference's checkCudaErrors called exit()).
+ */
+#ifndef CTGB_H_
+#define CTGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A cudaStream_t, declared without including the CUDA headers. */
+typedef struct CUstream_st *ct_stream;
+
+typedef enum ct_status {
+    CT_OK = 0,
+    CT_ERR_INVALID_ARGUMENT = 1, /* bad geometry, sizes or enum values */
+    CT_ERR_NULL_POINTER = 2,     /* a required pointer was NULL */
+    CT_ERR_WORKSPACE = 3,        /* workspace given but smaller than required */
+    CT_ERR_CUDA = 4,             /* a CUDA runtime call or launch failed */
+    CT_ERR_ALLOC = 5,            /* device or host allocation failed */
+    CT_ERR_UNSUPPORTED = 6,      /* valid request this build cannot run */
+    CT_ERR_TIMEOUT = 7           /* a bounded device-side wait gave up */
+} ct_status;
+
+/* Fan-beam geometry decoded from the reference's 16-float `parameter`
+ * attribute.  Field meanings and the float arithmetic of the derived fields
+ * follow the op constructors exactly: FP/transform.cc:59-76,
+ * BP/transform.cc:55-72, FBP/transform.cc:55-72, FDK/FBP.cc:61-84.
+ * (PI there is the float literal 3.14159265359f, GPURecon_GPU.h:3.) */
+typedef struct ct_fan_geom {
+    /* raw attribute values */
+    float sdd;           /* parameter[0]  source-detector distance D (mm)     */
+    float sid;           /* parameter[1]  source-isocentre distance R (mm)    */
+    int32_t n_views;     /* int(parameter[2])                                  */
+    float full_angle;    /* parameter[3]  angular range (degrees)             */
+    int32_t n_cols;      /* int(parameter[4]) detector channels                */
+    int32_t nx;          /* int(parameter[5])                                  */
+    int32_t ny;          /* int(parameter[6])                                  */
+    float rfov;          /* parameter[7]  reconstruction FOV radius (mm)      */
+    float shift;         /* parameter[9]  detector shift (channels; BP/FBP/FDK only) */
+    int32_t n_slices;    /* int(parameter[11]) slices per call in the ref op   */
+    float det_bottom;    /* parameter[13] FDK op only                          */
+    float drow;          /* parameter[14] FDK op only                          */
+    float dz;            /* parameter[15] FDK op only                          */
+    /* derived, in float, exactly as the reference constructors compute them */
+    float d_angle;       /* full_angle / n_views * PI / 180 (rad)              */
+    float dx, dy;        /* 2 * rfov / nx, 2 * rfov / ny (mm)                  */
+    float xmin, ymin;    /* -0.5 * nx * dx, -0.5 * ny * dy (mm)                */
+    float dcol;          /* parameter[8]  * PI / 180 (rad per channel)         */
+    float left;          /* parameter[10] * PI / 180 (rad, detector left edge) */
+    float start_angle;   /* parameter[12] * PI / 180 (decoded, unused by all ops) */
+} ct_fan_geom;
+
+/* Ramp-filter window of the FBP / FDK filter. */
+typedef enum ct_filter_window {
+    /* The reference kernel: Hsieh's h'' equiangular Ram-Lak form, 0.5 factor
+     * for 360-degree redundancy, scaled by R*d_angle*dcol
+     * (FBP/transform.cu:149-162, FDK/GPURecon_GPU.cu:184-200). */
+    CT_WINDOW_RAMLAK = 0,
+    /* Shepp-Logan: the parallel-beam Shepp-Logan taps 2/(pi^2 tau^2 (1-4n^2))
+     * with tau = dcol, mapped to the equiangular fan by (n dcol / sin(n dcol))^2,
+     * same 0.5 factor and R*d_angle*dcol scale.  config.py:42 names it
+     * (FilterType=1 "S-L") but no reference op reads it. */
+    CT_WINDOW_SHEPP_LOGAN = 1
+} ct_filter_window;
+
+/* How the row filter executes on the device. */
+typedef enum ct_filter_algo {
+    CT_FILTER_AUTO = 0,      /* the library picks (measured fastest accurate path) */
+    CT_FILTER_DIRECT = 1,    /* FP32 direct convolution, odd taps only */
+    CT_FILTER_TOEPLITZ_TC = 2 /* Toeplitz GEMM on tcgen05 tensor cores, BF16x3 split */
+} ct_filter_algo;
+
+typedef struct ct_plan_opts {
+    int32_t filter_window;  /* ct_filter_window */
+    int32_t filter_algo;    /* ct_filter_algo   */
+    int32_t reserved[6];    /* must be zero      */
+} ct_plan_opts;
+
+/* Operators, for ct_workspace_size. */
+typedef enum ct_op {
+    CT_OP_FP = 0,
+    CT_OP_FP_ADJOINT = 1,
+    CT_OP_BP = 2,
+    CT_OP_FBP = 3,
+    CT_OP_FBP_ADJOINT = 4,
+    CT_OP_FDK_BP = 5,
+    CT_OP_BP_ADJOINT = 6
+} ct_op;
+
+typedef struct ct_plan ct_plan;
+
+/* ---- status / build info ------------------------------------------------ */
+
+const char *ct_status_string(ct_status status);
+const char *ct_version(void);
+/* Last CUDA error text seen by this thread ("" if none). */
+const char *ct_last_error(void);
+/* Number of kernels this library has launched in this process. */
+uint64_t ct_launch_count(void);
+
+/* ---- geometry ------------------------------------------------------------ */
+
+/* Decodes the 16-float parameter vector.  Replaces the attr decoding of
+ * FPFanCurveOp / BPFanCurveOp / FBPFanCurveOp / BackProjectionOp
+ * (FP/transform.cc:59-76, BP/transform.cc:55-72, FBP/transform.cc:55-72,
+ * FDK/FBP.cc:61-84).  Host-only; needs no GPU. */
+ct_status ct_geom_from_param16(const float param[16], ct_fan_geom *out);
+
+/* The forward projector's per-ray table, evaluated on the host in FP64 exactly
+ * as plans build it: for ray (v, i), v-major, ray4[4r..4r+3] = start x, start y,
+ * step x, step y in texture pixel coordinates and nsamp[r] = floor(chord/0.125)
+ * (0 for rays missing the FOV).  Restates
+ * GenerateRayTraceMap_FB_ReconImage_OneView_kernel (FP/transform.cu:64-101).
+ * ray4 holds 4*n_views*n_cols floats, nsamp n_views*n_cols.  Needs no GPU. */
+ct_status ct_fp_ray_table(const ct_fan_geom *geom, const float *angles, int n_angles,
+                          float *ray4, int32_t *nsamp);
+
+/* ---- plans ----------------------------------------------------------------- */
+
+/* Builds the per-view (FP64-derived) geometry tables on the current device.
+ * `angles` is the host float32 array of n_angles view angles in radians (the
+ * `angle` attr, utils.py:49-54); n_angles must equal geom->n_views.
+ * Replaces para_setup_fan_curve (FP/transform.cu:20-62, BP/transform.cu:20-64,
+ * FBP/transform.cu:23-58) and the constructors' angle copy
+ * (FP/transform.cc:81-90).  opts may be NULL. */
+ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_angles,
+                         const ct_plan_opts *opts, ct_plan **out);
+ct_status ct_plan_destroy(ct_plan *plan);
+/* The geometry a plan was built from. */
+ct_status ct_plan_geom(const ct_plan *plan, ct_fan_geom *out);
+
+/* Device scratch bytes an operator needs for `batch` slices.  Operators that
+ * take d_work accept d_work == NULL, in which case they allocate the scratch
+ * stream-ordered (cudaMallocAsync/cudaFreeAsync) on `stream`. */
+ct_status ct_workspace_size(const ct_plan *plan, ct_op op, int batch, size_t *bytes);
+
+/* ---- fan-beam operators ---------------------------------------------------- */
+
+/* Ray-driven forward projection, d_img [batch][ny][nx] -> d_sino
+ * [batch][n_views][n_cols].  Per ray: the FOV-chord sample rule
+ * floor(chord/0.125 px), a left Riemann sum of bilinear, clamp-to-edge image
+ * samples, times 0.125*dx; rays missing the FOV give 0.  Bilinear weights are
+ * full FP32 (the reference used 8-bit texture weights).
+ * Replaces project_fan_curve (FP/transform.cu:173-269) with its kernels
+ * GenerateRayTraceMap_FB_ReconImage_OneView_kernel (:64-101) and
+ * RayTrace_ReconImage_OneView_kernel (:103-146). */
+ct_status ct_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                    void *d_work, size_t work_bytes, ct_stream stream);
+
+/* Exact adjoint (transpose) of ct_fp_fan: d_sino [batch][n_views][n_cols] ->
+ * d_img [batch][ny][nx].  No counterpart in the reference (it registers no
+ * gradient, utils.py:5). */
+ct_status ct_fp_fan_adjoint(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                            void *d_work, size_t work_bytes, ct_stream stream);
+
+/* Unweighted pixel-driven backprojection: for every pixel inside the FOV disc
+ * and every view, adds the linearly interpolated (clamped) detector value at
+ * col = (atan(t/U) - left)/dcol + shift when 0 < col < n_cols.
+ * Replaces backproject_fan_curve (BP/transform.cu:123-176) and
+ * BackProjOneView_fan_curve_kernel (BP/transform.cu:67-95). */
+ct_status ct_bp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                    ct_stream stream);
+
+/* Exact adjoint of ct_bp_fan: d_img [batch][ny][nx] -> d_sino
+ * [batch][n_views][n_cols].  No counterpart in the reference. */
+ct_status ct_bp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                            ct_stream stream);
+
+/* Row ramp filter only: each detector row of d_sino is convolved with the
+ * plan's window (middle n_cols samples of the full linear convolution).
+ * d_out may not alias d_sino.  Replaces the host ippsConv_32f loop
+ * (FBP/transform.cu:147-174).  The filter is symmetric, so it is its own
+ * adjoint. */
+ct_status ct_ramp_filter(const ct_plan *plan, const float *d_sino, float *d_out, int rows,
+                         ct_stream stream);
+
+/* Filtered backprojection: ramp filter, then BP weighted by 1/(U^2+t^2).
+ * Replaces backproject_fan_curve of FBP/transform.cu:117-201 (kernel :61-89). */
+ct_status ct_fbp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                     void *d_work, size_t work_bytes, ct_stream stream);
+
+/* Exact adjoint of ct_fbp_fan: d_img [batch][ny][nx] -> d_sino
+ * [batch][n_views][n_cols] (weighted-BP transpose, then the filter).
+ * No counterpart in the reference. */
+ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                             void *d_work, size_t work_bytes, ct_stream stream);
+
+/* The reference "BackProjection" op of FDK/FBP.cc (nZ = 1, nRows = 1,
+ * FDK/FBP.cc:85,98): ramp filter, then the CB_EA backprojection kernel with
+ * 1/L^2 weight and detector shift (FDK/GPURecon_GPU.cu:15-50,163-268).  With
+ * one detector row its result equals ct_fbp_fan; unlike the reference, every
+ * one of the `batch` slices is processed (the reference copied only the first,
+ * FDK/GPURecon_GPU.cu:178-179) and the output is zeroed first. */
+ct_status ct_fdk_bp(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                    void *d_work, size_t work_bytes, ct_stream stream);
+
+/* ---- the plain per-view launch loop (comparison baseline) ----------------- */
+
+/* The reference's execution structure on the same GPU: for each slice and
+ * each view one kernel launch followed by a stream synchronisation
+ * (FP/transform.cu:162-169, BP/transform.cu:110-119), with explicit FP32
+ * lerp instead of texture references.  Same results as the fused operators;
+ * kept only to measure against. */
+ct_status ct_plain_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
+                          ct_stream stream);
+ct_status ct_plain_fp_fan_adjoint(const ct_plan *plan, const float *d_sino, float *d_img,
+                                  int batch, ct_stream stream);
+ct_status ct_plain_bp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
+                          ct_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTGB_H_ */

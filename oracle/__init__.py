@@ -1,0 +1,223 @@
+"""FP64 CPU oracle of the reference's FP / BP / FBP / FDK operators.
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline legs of ``bench.py`` import this package, and only as the checker
+or the timed CPU reference; the product path never calls it.
+
+Parity status: unpinned against reference outputs (the reference cannot be
+built and has no golden vectors); pinned to the reference's executed Python
+geometry packing and to exact / analytic known answers (see ``oracle.c``).
+
+The C restatement (``oracle.c``) is compiled with gcc + OpenMP into
+``oracle/_build/liboracle.so`` on first use (``build()``).
+"""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+_DIR = Path(__file__).resolve().parent
+_SRC = _DIR / "oracle.c"
+_BUILD = _DIR / "_build"
+_LIB = _BUILD / "liboracle.so"
+_CFLAGS = ["-O2", "-fopenmp", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra", "-shared"]
+
+RAMLAK = 0
+SHEPP_LOGAN = 1
+
+
+class OrcGeom(ctypes.Structure):
+    _fields_ = [
+        ("sdd", ctypes.c_float), ("sid", ctypes.c_float), ("n_views", ctypes.c_int32),
+        ("full_angle", ctypes.c_float), ("n_cols", ctypes.c_int32), ("nx", ctypes.c_int32),
+        ("ny", ctypes.c_int32), ("rfov", ctypes.c_float), ("shift", ctypes.c_float),
+        ("n_slices", ctypes.c_int32), ("det_bottom", ctypes.c_float), ("drow", ctypes.c_float),
+        ("dz", ctypes.c_float), ("d_angle", ctypes.c_float), ("dx", ctypes.c_float),
+        ("dy", ctypes.c_float), ("xmin", ctypes.c_float), ("ymin", ctypes.c_float),
+        ("dcol", ctypes.c_float), ("left", ctypes.c_float), ("start_angle", ctypes.c_float),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def build(force: bool = False) -> Path:
+    """Compiles liboracle.so (gcc, OpenMP) if missing or stale."""
+    _BUILD.mkdir(parents=True, exist_ok=True)
+    stamp = _BUILD / "stamp.txt"
+    fp = hashlib.sha256(_SRC.read_bytes() + " ".join(_CFLAGS).encode()
+                        + os.uname().machine.encode()).hexdigest()
+    if not force and _LIB.exists() and stamp.exists() and stamp.read_text() == fp:
+        return _LIB
+    tmp = _BUILD / "liboracle.so.tmp"
+    cmd = ["gcc", *_CFLAGS, str(_SRC), "-o", str(tmp), "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{res.stderr}")
+    os.replace(tmp, _LIB)
+    stamp.write_text(fp)
+    return _LIB
+
+
+_lib = None
+
+
+def _l():
+    global _lib
+    if _lib is None:
+        lib = ctypes.CDLL(str(build()))
+        P = ctypes.POINTER
+        dp, fp_, ip = P(ctypes.c_double), P(ctypes.c_float), P(ctypes.c_int32)
+        g = P(OrcGeom)
+        lib.orc_decode_param16.argtypes = [fp_, g]
+        lib.orc_decode_param16.restype = ctypes.c_int
+        lib.orc_set_texture_emulation.argtypes = [ctypes.c_int]
+        lib.orc_ray_table.argtypes = [g, fp_, dp, ip]
+        lib.orc_fp_fan.argtypes = [g, fp_, dp, dp, ctypes.c_int]
+        lib.orc_fp_fan_adjoint.argtypes = [g, fp_, dp, dp, ctypes.c_int]
+        lib.orc_bp_fan.argtypes = [g, fp_, dp, dp, ctypes.c_int, ctypes.c_int]
+        lib.orc_bp_fan_transpose.argtypes = [g, fp_, dp, dp, ctypes.c_int, ctypes.c_int]
+        lib.orc_ramp_taps.argtypes = [g, ctypes.c_int, dp]
+        lib.orc_ramp_filter.argtypes = [g, ctypes.c_int, dp, dp, ctypes.c_long]
+        lib.orc_fbp_fan.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
+        lib.orc_fbp_fan_adjoint.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
+        lib.orc_fdk_bp.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
+        _lib = lib
+    return _lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _angles(g: OrcGeom, angles) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(angles, dtype=np.float32))
+    if a.shape != (g.n_views,):
+        raise ValueError(f"angles must have shape ({g.n_views},), got {a.shape}")
+    return a
+
+
+def decode(param16) -> OrcGeom:
+    p = np.ascontiguousarray(np.asarray(param16, dtype=np.float32))
+    if p.shape != (16,):
+        raise ValueError("parameter vector must have 16 entries")
+    g = OrcGeom()
+    if _l().orc_decode_param16(_fptr(p), ctypes.byref(g)) != 0:
+        raise ValueError("invalid parameter vector")
+    return g
+
+
+def set_texture_emulation(on: bool) -> None:
+    _l().orc_set_texture_emulation(1 if on else 0)
+
+
+def ray_table(g: OrcGeom, angles):
+    a = _angles(g, angles)
+    R = g.n_views * g.n_cols
+    ray = np.zeros((R, 4), np.float64)
+    ns = np.zeros(R, np.int32)
+    _l().orc_ray_table(ctypes.byref(g), _fptr(a), _dptr(ray),
+                       ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    return ray.reshape(g.n_views, g.n_cols, 4), ns.reshape(g.n_views, g.n_cols)
+
+
+def _batch_img(g, img):
+    x = _f64(img)
+    if x.ndim == 2:
+        x = x[None]
+    if x.shape[1:] != (g.ny, g.nx):
+        raise ValueError(f"image must be [B,{g.ny},{g.nx}], got {x.shape}")
+    return x
+
+
+def _batch_sino(g, sino):
+    y = _f64(sino)
+    if y.ndim == 2:
+        y = y[None]
+    if y.shape[1:] != (g.n_views, g.n_cols):
+        raise ValueError(f"sinogram must be [B,{g.n_views},{g.n_cols}], got {y.shape}")
+    return y
+
+
+def fp_fan(g, angles, img) -> np.ndarray:
+    x = _batch_img(g, img)
+    out = np.zeros((x.shape[0], g.n_views, g.n_cols), np.float64)
+    _l().orc_fp_fan(ctypes.byref(g), _fptr(_angles(g, angles)), _dptr(x), _dptr(out), x.shape[0])
+    return out
+
+
+def fp_fan_adjoint(g, angles, sino) -> np.ndarray:
+    y = _batch_sino(g, sino)
+    out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
+    _l().orc_fp_fan_adjoint(ctypes.byref(g), _fptr(_angles(g, angles)), _dptr(y), _dptr(out),
+                            y.shape[0])
+    return out
+
+
+def bp_fan(g, angles, sino, weighted: bool = False) -> np.ndarray:
+    y = _batch_sino(g, sino)
+    out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
+    _l().orc_bp_fan(ctypes.byref(g), _fptr(_angles(g, angles)), _dptr(y), _dptr(out), y.shape[0],
+                    1 if weighted else 0)
+    return out
+
+
+def bp_fan_transpose(g, angles, img, weighted: bool = False) -> np.ndarray:
+    x = _batch_img(g, img)
+    out = np.zeros((x.shape[0], g.n_views, g.n_cols), np.float64)
+    _l().orc_bp_fan_transpose(ctypes.byref(g), _fptr(_angles(g, angles)), _dptr(x), _dptr(out),
+                              x.shape[0], 1 if weighted else 0)
+    return out
+
+
+def ramp_taps(g, window: int = RAMLAK) -> np.ndarray:
+    t = np.zeros(2 * g.n_cols - 1, np.float64)
+    _l().orc_ramp_taps(ctypes.byref(g), window, _dptr(t))
+    return t
+
+
+def ramp_filter(g, sino, window: int = RAMLAK) -> np.ndarray:
+    y = _f64(sino)
+    if y.shape[-1] != g.n_cols:
+        raise ValueError("last axis must be n_cols")
+    out = np.zeros_like(y)
+    rows = y.size // g.n_cols
+    _l().orc_ramp_filter(ctypes.byref(g), window, _dptr(y), _dptr(out), rows)
+    return out
+
+
+def fbp_fan(g, angles, sino, window: int = RAMLAK) -> np.ndarray:
+    y = _batch_sino(g, sino)
+    out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
+    _l().orc_fbp_fan(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(y), _dptr(out),
+                     y.shape[0])
+    return out
+
+
+def fbp_fan_adjoint(g, angles, img, window: int = RAMLAK) -> np.ndarray:
+    x = _batch_img(g, img)
+    out = np.zeros((x.shape[0], g.n_views, g.n_cols), np.float64)
+    _l().orc_fbp_fan_adjoint(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(x),
+                             _dptr(out), x.shape[0])
+    return out
+
+
+def fdk_bp(g, angles, sino, window: int = RAMLAK) -> np.ndarray:
+    y = _batch_sino(g, sino)
+    out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
+    _l().orc_fdk_bp(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(y), _dptr(out),
+                    y.shape[0])
+    return out

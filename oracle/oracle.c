@@ -1,0 +1,453 @@
+/*
+ * oracle.c -- FP64 CPU restatement of FanBeamCTRecon_TensorflowOp's four
+ * operators.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and
+ * the CPU-baseline leg of the benchmark call it as the checker; no product
+ * code path links or executes it.
+ *
+ * Parity status: UNPINNED against the reference's own outputs.  The reference
+ * cannot be built here (legacy texture references do not compile with CUDA 13;
+ * TensorFlow, Intel IPP and helper_cuda.h are absent) and ships no tests,
+ * golden vectors or fixtures (its only input, test.fbp, is missing).  What
+ * pins this restatement instead: the reference's own Python geometry packing
+ * (utils.py, config.py) executed to produce golden parameter/angle vectors,
+ * exact known answers of the discrete operators (constant image, constant
+ * sinogram), analytic ellipse line integrals, and FP64 adjoint identities.
+ *
+ * Every function follows the reference's arithmetic in double precision,
+ * citing the file:line it restates.  Geometry decoding stays in float, as the
+ * op constructors do it, because those floats are the op's attributes.
+ *
+ * Optional texture emulation (orc_set_texture_emulation(1)) quantises the
+ * linear-filter fractions to 8 fractional bits, the documented precision of
+ * CUDA's hardware texture filtering, to bound how far the reference's
+ * texture-unit outputs sit from exact bilinear interpolation.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_PI_F 3.14159265359f /* FP/transform.h:1 */
+#define ORC_STEP 0.125          /* FP/transform.cu:10 */
+
+typedef struct orc_geom {
+    float sdd, sid;
+    int32_t n_views;
+    float full_angle;
+    int32_t n_cols, nx, ny;
+    float rfov, shift;
+    int32_t n_slices;
+    float det_bottom, drow, dz;
+    float d_angle, dx, dy, xmin, ymin, dcol, left, start_angle;
+} orc_geom;
+
+static int g_tex8 = 0;
+
+void orc_set_texture_emulation(int on) { g_tex8 = on ? 1 : 0; }
+
+static double frac_w(double f) {
+    /* 8 fractional bits, round to nearest (texture filtering precision) */
+    return g_tex8 ? floor(f * 256.0 + 0.5) / 256.0 : f;
+}
+
+/* FP/transform.cc:59-76 (FDK/FBP.cc:61-84 for the last three) */
+int orc_decode_param16(const float *p, orc_geom *g) {
+    memset(g, 0, sizeof(*g));
+    if (!isfinite(p[2]) || !isfinite(p[4]) || !isfinite(p[5]) || !isfinite(p[6]) ||
+        !isfinite(p[11]))
+        return 1;
+    g->sdd = p[0];
+    g->sid = p[1];
+    g->n_views = (int32_t)p[2];
+    g->full_angle = p[3];
+    g->n_cols = (int32_t)p[4];
+    g->nx = (int32_t)p[5];
+    g->ny = (int32_t)p[6];
+    g->rfov = p[7];
+    g->shift = p[9];
+    g->n_slices = (int32_t)p[11];
+    g->det_bottom = p[13];
+    g->drow = p[14];
+    g->dz = p[15];
+    if (g->n_views <= 0 || g->nx <= 0 || g->ny <= 0) return 1;
+    {
+        float a = g->full_angle / (float)g->n_views;
+        a = a * ORC_PI_F;
+        g->d_angle = a / 180.0f;
+    }
+    {
+        float two_r = 2.0f * g->rfov;
+        float hx, hy;
+        g->dx = two_r / (float)g->nx;
+        g->dy = two_r / (float)g->ny;
+        hx = -0.5f * (float)g->nx;
+        hy = -0.5f * (float)g->ny;
+        g->xmin = hx * g->dx;
+        g->ymin = hy * g->dy;
+    }
+    {
+        float t = p[8] * ORC_PI_F;
+        g->dcol = t / 180.0f;
+        t = p[10] * ORC_PI_F;
+        g->left = t / 180.0f;
+        t = p[12] * ORC_PI_F;
+        g->start_angle = t / 180.0f;
+    }
+    return 0;
+}
+
+/* GenerateRayTraceMap_FB_ReconImage_OneView_kernel, FP/transform.cu:64-101:
+ * ray angle beta + left + (i+1/2) dcol; distance R/dx*sin(gamma) of the ray
+ * from the isocentre; intersections with the FOV circle of radius rfov/dx;
+ * n = floor(chord/0.125); start shifted by rfov/dx into texture coordinates.
+ * A ray missing the circle gets n = 0 (the reference's sqrtf(negative) = NaN
+ * converts to 0 samples). */
+void orc_ray_table(const orc_geom *g, const float *angles, double *ray, int32_t *nsamp) {
+    const int V = g->n_views, C = g->n_cols;
+    const double dx = g->dx;
+    const double src = (double)g->sid / dx, fov = (double)g->rfov / dx;
+    const double left = g->left, dcol = g->dcol;
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < V; ++v) {
+        const double beta = angles[v];
+        for (int i = 0; i < C; ++i) {
+            const size_t r = (size_t)v * C + i;
+            double *q = ray + 4 * r;
+            const double gam = left + (i + 0.5) * dcol;
+            const double th = beta + gam;
+            const double sn = sin(th), cs = cos(th);
+            const double dist = src * sin(gam);
+            const double h = fov * fov - dist * dist;
+            double x1, x2, y1, y2, ax, ay, bx, by, L, nn;
+            q[0] = q[1] = q[2] = q[3] = 0.0;
+            nsamp[r] = 0;
+            if (!(h > 0.0)) continue;
+            x1 = -sqrt(h);
+            x2 = -x1;
+            y1 = -dist;
+            y2 = -dist;
+            ax = x1 * cs - y1 * sn;
+            ay = x1 * sn + y1 * cs;
+            bx = x2 * cs - y2 * sn;
+            by = x2 * sn + y2 * cs;
+            L = sqrt((ax - bx) * (ax - bx) + (ay - by) * (ay - by));
+            nn = floor(L / ORC_STEP);
+            if (!(nn >= 1.0)) continue;
+            nsamp[r] = (int32_t)nn;
+            q[0] = ax + fov;
+            q[1] = ay + fov;
+            q[2] = (bx - ax) / nn;
+            q[3] = (by - ay) / nn;
+        }
+    }
+}
+
+/* tex2D with cudaFilterModeLinear + cudaAddressModeClamp on an nx-by-ny float
+ * array: texel (i, j) centred at (i+1/2, j+1/2), clamp-to-edge taps. */
+typedef struct tap4 {
+    int i0, i1, j0, j1;
+    double w00, w10, w01, w11;
+} tap4;
+
+static tap4 bilinear_taps(int nx, int ny, double x, double y) {
+    tap4 t;
+    const double xb = x - 0.5, yb = y - 0.5;
+    const double fx = floor(xb), fy = floor(yb);
+    const double ax = frac_w(xb - fx), ay = frac_w(yb - fy);
+    const int i = (int)fx, j = (int)fy;
+    t.i0 = i < 0 ? 0 : (i > nx - 1 ? nx - 1 : i);
+    t.i1 = i + 1 < 0 ? 0 : (i + 1 > nx - 1 ? nx - 1 : i + 1);
+    t.j0 = j < 0 ? 0 : (j > ny - 1 ? ny - 1 : j);
+    t.j1 = j + 1 < 0 ? 0 : (j + 1 > ny - 1 ? ny - 1 : j + 1);
+    t.w00 = (1.0 - ax) * (1.0 - ay);
+    t.w10 = ax * (1.0 - ay);
+    t.w01 = (1.0 - ax) * ay;
+    t.w11 = ax * ay;
+    return t;
+}
+
+/* RayTrace_ReconImage_OneView_kernel, FP/transform.cu:103-146:
+ * p = 0.125 * dx * sum_{k<n} tex2D(start + k*step). */
+void orc_fp_fan(const orc_geom *g, const float *angles, const double *img, double *sino,
+                int batch) {
+    const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
+    const size_t R = (size_t)V * C;
+    double *ray = (double *)malloc(sizeof(double) * 4 * R);
+    int32_t *ns = (int32_t *)malloc(sizeof(int32_t) * R);
+    const double w = ORC_STEP * (double)g->dx;
+    orc_ray_table(g, angles, ray, ns);
+    for (int b = 0; b < batch; ++b) {
+        const double *im = img + (size_t)b * nx * ny;
+        double *out = sino + (size_t)b * R;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long r = 0; r < (long)R; ++r) {
+            const double *q = ray + 4 * r;
+            double acc = 0.0;
+            for (int k = 0; k < ns[r]; ++k) {
+                const tap4 t = bilinear_taps(nx, ny, q[0] + k * q[2], q[1] + k * q[3]);
+                acc += t.w00 * im[t.j0 * nx + t.i0] + t.w10 * im[t.j0 * nx + t.i1] +
+                       t.w01 * im[t.j1 * nx + t.i0] + t.w11 * im[t.j1 * nx + t.i1];
+            }
+            out[r] = acc * w;
+        }
+    }
+    free(ray);
+    free(ns);
+}
+
+/* Exact transpose of orc_fp_fan (no reference counterpart). */
+void orc_fp_fan_adjoint(const orc_geom *g, const float *angles, const double *sino, double *img,
+                        int batch) {
+    const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
+    const size_t R = (size_t)V * C, N = (size_t)nx * ny;
+    double *ray = (double *)malloc(sizeof(double) * 4 * R);
+    int32_t *ns = (int32_t *)malloc(sizeof(int32_t) * R);
+    const double w = ORC_STEP * (double)g->dx;
+    orc_ray_table(g, angles, ray, ns);
+    memset(img, 0, sizeof(double) * N * batch);
+    for (int b = 0; b < batch; ++b) {
+        const double *in = sino + (size_t)b * R;
+        double *im = img + (size_t)b * N;
+        /* each thread scatters into a private image; the images are summed */
+#pragma omp parallel
+        {
+            double *priv = (double *)calloc(N, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+            for (long r = 0; r < (long)R; ++r) {
+                const double *q = ray + 4 * r;
+                const double val = in[r] * w;
+                if (val == 0.0) continue;
+                for (int k = 0; k < ns[r]; ++k) {
+                    const tap4 t = bilinear_taps(nx, ny, q[0] + k * q[2], q[1] + k * q[3]);
+                    priv[t.j0 * nx + t.i0] += val * t.w00;
+                    priv[t.j0 * nx + t.i1] += val * t.w10;
+                    priv[t.j1 * nx + t.i0] += val * t.w01;
+                    priv[t.j1 * nx + t.i1] += val * t.w11;
+                }
+            }
+#pragma omp critical
+            for (size_t p = 0; p < N; ++p) im[p] += priv[p];
+            free(priv);
+        }
+    }
+    free(ray);
+    free(ns);
+}
+
+/* Pixel geometry shared by the BP family (BP/transform.cu:76-92,116;
+ * FBP/transform.cu:70-87; FDK/GPURecon_GPU.cu:25-49). Returns 1 when the
+ * detector coordinate lies in (0, C) and fills the taps/weight. */
+static int bp_col(const orc_geom *g, double x, double y, double c, double s, int *i0, int *i1,
+                  double *f, double *U_out, double *t_out) {
+    const double U = (double)g->sid + x * c + y * s;
+    const double t = -x * s + y * c;
+    const double col = (atan(t / U) - (double)g->left) / (double)g->dcol + (double)g->shift;
+    *U_out = U;
+    *t_out = t;
+    if (!(col > 0.0 && col < (double)g->n_cols)) return 0;
+    {
+        const double cb = col - 0.5;
+        const double fi = floor(cb);
+        const int i = (int)fi;
+        *f = frac_w(cb - fi);
+        *i0 = i < 0 ? 0 : i;
+        *i1 = i + 1 > g->n_cols - 1 ? g->n_cols - 1 : i + 1;
+    }
+    return 1;
+}
+
+/* BackProjOneView_fan_curve_kernel summed over views (BP/transform.cu:67-95,
+ * 110-119); weighted != 0 adds the 1/(U^2+t^2) factor of FBP/transform.cu:78. */
+void orc_bp_fan(const orc_geom *g, const float *angles, const double *sino, double *img,
+                int batch, int weighted) {
+    const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
+    const double r2 = (double)g->rfov * (double)g->rfov;
+    for (int b = 0; b < batch; ++b) {
+        const double *sb = sino + (size_t)b * V * C;
+        double *im = img + (size_t)b * nx * ny;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int j = 0; j < ny; ++j) {
+            const double y = (double)g->ymin + (double)g->dy * (j + 0.5);
+            for (int i = 0; i < nx; ++i) {
+                const double x = (double)g->xmin + (double)g->dx * (i + 0.5);
+                double acc = 0.0;
+                if (x * x + y * y <= r2) {
+                    for (int v = 0; v < V; ++v) {
+                        const double beta = angles[v];
+                        const double c = -cos(beta), s = -sin(beta);
+                        int i0, i1;
+                        double f, U, t;
+                        if (bp_col(g, x, y, c, s, &i0, &i1, &f, &U, &t)) {
+                            const double *row = sb + (size_t)v * C;
+                            double val = (1.0 - f) * row[i0] + f * row[i1];
+                            if (weighted) val *= 1.0 / (U * U + t * t);
+                            acc += val;
+                        }
+                    }
+                }
+                im[(size_t)j * nx + i] = acc;
+            }
+        }
+    }
+}
+
+/* Transpose of orc_bp_fan (no reference counterpart). */
+void orc_bp_fan_transpose(const orc_geom *g, const float *angles, const double *img,
+                          double *sino, int batch, int weighted) {
+    const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
+    const double r2 = (double)g->rfov * (double)g->rfov;
+    memset(sino, 0, sizeof(double) * (size_t)batch * V * C);
+    for (int b = 0; b < batch; ++b) {
+        const double *im = img + (size_t)b * nx * ny;
+        double *sb = sino + (size_t)b * V * C;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int v = 0; v < V; ++v) {
+            const double beta = angles[v];
+            const double c = -cos(beta), s = -sin(beta);
+            double *row = sb + (size_t)v * C;
+            for (int j = 0; j < ny; ++j) {
+                const double y = (double)g->ymin + (double)g->dy * (j + 0.5);
+                for (int i = 0; i < nx; ++i) {
+                    const double x = (double)g->xmin + (double)g->dx * (i + 0.5);
+                    int i0, i1;
+                    double f, U, t, val;
+                    if (!(x * x + y * y <= r2)) continue;
+                    val = im[(size_t)j * nx + i];
+                    if (val == 0.0) continue;
+                    if (!bp_col(g, x, y, c, s, &i0, &i1, &f, &U, &t)) continue;
+                    if (weighted) val *= 1.0 / (U * U + t * t);
+                    row[i0] += val * (1.0 - f);
+                    row[i1] += val * f;
+                }
+            }
+        }
+    }
+}
+
+/* Ramp taps, index n + C - 1 (FBP/transform.cu:149-162; FDK/GPURecon_GPU.cu:
+ * 184-200).  window 0: the reference's Hsieh h'' Ram-Lak form with the 0.5
+ * factor; window 1: Shepp-Logan 0.5*2/(pi^2 dcol^2 (1-4n^2)) times
+ * (n dcol/sin(n dcol))^2.  Scaled by R * d_angle * dcol. */
+void orc_ramp_taps(const orc_geom *g, int window, double *taps) {
+    const int C = g->n_cols;
+    const double pi = (double)ORC_PI_F, dc = g->dcol;
+    const double scale = (double)g->sid * (double)g->d_angle * dc;
+    for (int n = -(C - 1); n <= C - 1; ++n) {
+        double h;
+        if (window == 1) {
+            if (n == 0) {
+                h = 0.5 * 2.0 / (pi * pi * dc * dc);
+            } else {
+                const double s = sin(n * dc);
+                h = 0.5 * 2.0 * (double)n * (double)n /
+                    (pi * pi * s * s * (1.0 - 4.0 * (double)n * (double)n));
+            }
+        } else if (n == 0) {
+            h = 0.5 / (4.0 * dc * dc);
+        } else if (n % 2 != 0) {
+            const double s = sin(n * dc);
+            h = -0.5 / (pi * pi * s * s);
+        } else {
+            h = 0.0;
+        }
+        taps[n + C - 1] = h * scale;
+    }
+}
+
+/* ippsConv_32f full linear convolution of each row with the 2C-1 taps,
+ * keeping samples C-1 .. 2C-2 (FBP/transform.cu:166-174):
+ * q[i] = sum_j p[j] * taps[i - j + C - 1]. */
+void orc_ramp_filter(const orc_geom *g, int window, const double *in, double *out, long rows) {
+    const int C = g->n_cols;
+    double *taps = (double *)malloc(sizeof(double) * (2 * (size_t)C - 1));
+    orc_ramp_taps(g, window, taps);
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < rows; ++r) {
+        const double *p = in + (size_t)r * C;
+        double *q = out + (size_t)r * C;
+        for (int i = 0; i < C; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < C; ++j) acc += p[j] * taps[i - j + C - 1];
+            q[i] = acc;
+        }
+    }
+    free(taps);
+}
+
+/* backproject_fan_curve of FBP/transform.cu:117-201: filter, then weighted BP. */
+void orc_fbp_fan(const orc_geom *g, const float *angles, int window, const double *sino,
+                 double *img, int batch) {
+    const size_t n = (size_t)batch * g->n_views * g->n_cols;
+    double *tmp = (double *)malloc(sizeof(double) * (n ? n : 1));
+    orc_ramp_filter(g, window, sino, tmp, (long)batch * g->n_views);
+    orc_bp_fan(g, angles, tmp, img, batch, 1);
+    free(tmp);
+}
+
+/* Transpose of orc_fbp_fan: weighted-BP transpose, then the (symmetric) filter. */
+void orc_fbp_fan_adjoint(const orc_geom *g, const float *angles, int window, const double *img,
+                         double *sino, int batch) {
+    const size_t n = (size_t)batch * g->n_views * g->n_cols;
+    double *tmp = (double *)malloc(sizeof(double) * (n ? n : 1));
+    orc_bp_fan_transpose(g, angles, img, tmp, batch, 1);
+    orc_ramp_filter(g, window, tmp, sino, (long)batch * g->n_views);
+    free(tmp);
+}
+
+/* The "BackProjection" op (FDK/FBP.cc:61-110 -> BP_One_Rot_3D_GPU,
+ * FDK/GPURecon_GPU.cu:163-268): filter each (view, row), then per view the
+ * CB_EA kernel (:15-50) over nz slices with row index
+ * ((z - z_src) * D / U - det_bottom) / drow on an n_rows-high view texture
+ * (clamped), weight 1/(U^2+t^2).  The op fixes nz = n_rows = 1
+ * (FDK/FBP.cc:85,98), zmin = -dz/2, z_src = 0 (FDK/GPURecon_GPU.cu:226). */
+void orc_fdk_bp(const orc_geom *g, const float *angles, int window, const double *sino,
+                double *img, int batch) {
+    const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
+    const int n_rows = 1, nz = 1;
+    const float zmin = -0.5f * g->dz * (float)nz;
+    const double r2 = (double)g->rfov * (double)g->rfov;
+    const size_t n = (size_t)batch * V * C;
+    double *filt = (double *)malloc(sizeof(double) * (n ? n : 1));
+    orc_ramp_filter(g, window, sino, filt, (long)batch * V * n_rows);
+    for (int b = 0; b < batch; ++b) {
+        const double *sb = filt + (size_t)b * V * C * n_rows;
+        double *im = img + (size_t)b * nx * ny * nz;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int j = 0; j < ny; ++j) {
+            const double y = (double)g->ymin + (double)g->dy * (j + 0.5);
+            for (int i = 0; i < nx; ++i) {
+                const double x = (double)g->xmin + (double)g->dx * (i + 0.5);
+                for (int k = 0; k < nz; ++k) {
+                    double acc = 0.0;
+                    const double zk = (double)zmin + (double)g->dz * (k + 0.5);
+                    if (x * x + y * y <= r2) {
+                        for (int v = 0; v < V; ++v) {
+                            const double beta = angles[v];
+                            const double c = -cos(beta), s = -sin(beta);
+                            int i0, i1;
+                            double f, U, t;
+                            if (bp_col(g, x, y, c, s, &i0, &i1, &f, &U, &t)) {
+                                const double row = ((zk - 0.0) * (double)g->sdd / U -
+                                                    (double)g->det_bottom) /
+                                                   (double)g->drow;
+                                const double rb = row - 0.5, rf = floor(rb);
+                                const double fr = frac_w(rb - rf);
+                                const int r0 = (int)rf;
+                                const int ra = r0 < 0 ? 0 : (r0 > n_rows - 1 ? n_rows - 1 : r0);
+                                const int rc =
+                                    r0 + 1 < 0 ? 0 : (r0 + 1 > n_rows - 1 ? n_rows - 1 : r0 + 1);
+                                const double *va = sb + ((size_t)v * n_rows + ra) * C;
+                                const double *vc = sb + ((size_t)v * n_rows + rc) * C;
+                                const double a = (1.0 - f) * va[i0] + f * va[i1];
+                                const double cval = (1.0 - f) * vc[i0] + f * vc[i1];
+                                acc += ((1.0 - fr) * a + fr * cval) / (U * U + t * t);
+                            }
+                        }
+                    }
+                    im[((size_t)k * ny + j) * nx + i] = acc;
+                }
+            }
+        }
+    }
+    free(filt);
+}

@@ -1,0 +1,58 @@
+"""Geometries of the parity tests, as 16-float parameter vectors + angles."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from fanbeamctrecon_tensorflowop_gb300.geometry import angle, fan_param16
+
+SID, SDD = 541.0, 949.0
+DCOL = 1.0 / 949.0  # 1 mm channel pitch at the detector, in rad
+
+
+def small(n=64, views=90, cols=96, pixel=2.8, shift=0.0, ny=None, full=360.0, batch=1):
+    """A small fan geometry whose detector covers the FOV."""
+    p = fan_param16(sdd=SDD, sid=SID, n_views=views, n_cols=cols, n=n, pixel_mm=pixel,
+                    dcol_rad=4.0 * DCOL, shift=shift, ny=ny, full_angle=full, batch=batch)
+    return p, angle(views, 0.0)
+
+
+def config0():
+    """256^2 at 1 mm, 720 views x 512 channels (the CPU-runnable workload)."""
+    p = fan_param16(sdd=SDD, sid=SID, n_views=720, n_cols=512, n=256, pixel_mm=1.0,
+                    dcol_rad=DCOL)
+    return p, angle(720, 0.0)
+
+
+def config1():
+    """512^2 at 0.7 mm, 984 views x 888 channels (the clinical-scale workload)."""
+    p = fan_param16(sdd=SDD, sid=SID, n_views=984, n_cols=888, n=512, pixel_mm=0.7,
+                    dcol_rad=DCOL)
+    return p, angle(984, 0.0)
+
+
+def fdk_driver(nview=96, ncol=888, nimg=64):
+    """The FDK driver's geometry (FDK/FDK_test_training.py:20-77) at reduced
+    view count / image size: SDD 946.73233346, SAD 538.52, 888 channels of
+    55.0059/888 deg, shift 1.125, left -27.50295 deg, rFOV 250, det_bottom
+    -35.16105, drow 1.0987828125, dz 2.5."""
+    p = np.arange(16, dtype=np.float32)
+    p[0] = 946.73233346
+    p[1] = 538.52
+    p[2] = nview
+    p[3] = nview * 360 / nview
+    p[4] = ncol
+    p[5] = nimg
+    p[6] = nimg
+    p[7] = 250
+    p[8] = 55.0059 / ncol
+    p[9] = 1.125
+    p[10] = -27.50295
+    p[11] = 1
+    p[12] = 0
+    p[13] = -35.16105
+    p[14] = 1.0987828125
+    p[15] = 2.5
+    a = (np.arange(nview) * (2.0 * math.pi / nview)).astype(np.float32)
+    return p, a
