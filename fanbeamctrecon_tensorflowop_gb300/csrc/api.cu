@@ -196,6 +196,7 @@ ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_ang
     p->filter_algo = CT_FILTER_DIRECT;
     p->fp_weight = (float)(CT_FP_STEP * (double)geom->dx);
     p->fov_r2 = geom->rfov * geom->rfov;
+    p->atan_deg = ct_fit_atan(1.02 * ct_max_tan_gamma(geom), p->atan_coef);
     p->total_samples = t.total_samples;
     p->max_nsamp = t.max_nsamp;
     p->h_view_cs = t.view_cs;

@@ -7,36 +7,65 @@
 // and when 0 < col < n_cols the pixel gains the linearly interpolated,
 // clamped detector value at col (texel centres at +1/2), times 1/(U^2+t^2) in
 // the weighted form (BP/transform.cu:76-92, FBP/transform.cu:70-87,
-// FDK/GPURecon_GPU.cu:25-49).  One launch covers all views and slices; each
-// thread keeps four pixels of a 32x32 tile in registers across all views, so
-// the image is written once instead of read-modified-written per view.
+// FDK/GPURecon_GPU.cu:25-49).
+//
+// One launch covers all views and slices.  Each thread keeps four pixels of a
+// 32x32 tile in registers across all views (the image is written once, not
+// read-modified-written per view), and evaluates the per-pixel geometry once
+// for up to four slices.  t/U uses the SFU reciprocal; atan(z) is a
+// polynomial in z^2 fitted per plan over the FOV's |z| range (to FP32 atanf
+// accuracy, 3e-8 absolute), with atanf kept for fans wider than 90 degrees.
 #include "common.cuh"
 
 namespace ctk {
 namespace {
 
-constexpr int kTile = 32;      // tile edge (pixels)
+constexpr int kTile = 32;       // tile edge (pixels)
 constexpr int kRowsPerThr = 4;  // 32x8 threads cover 32x32 pixels
 
 struct BpArgs {
     int V, C, nx, ny;
     float xmin, ymin, dx, dy;
-    float R, left, dcol, shift;
+    float R;
+    float inv_dcol;   // 1/dcol
+    float pos_off;    // shift - left/dcol + 1/2: y = atan*inv_dcol + pos_off = col + 1/2
+    float fC;         // n_cols
     double fov_r2;
+    float coef[9];    // atan(z) = z * sum coef[k] z^(2k)
 };
 
-template <bool WEIGHTED>
+template <int DEG>
+__device__ __forceinline__ float fov_atan(float z, const float *c) {
+    if constexpr (DEG == 0) {
+        return atanf(z);
+    } else {
+        const float s = z * z;
+        float p = c[DEG];
+#pragma unroll
+        for (int k = DEG - 1; k >= 0; --k) p = fmaf(p, s, c[k]);
+        return z * p;
+    }
+}
+
+// y = col + 1/2 >= 0: i = trunc(y) = floor(col - 1/2) + 1 and f = frac(y),
+// without float-to-int conversion instructions (valid for 0 <= y < 2^22).
+__device__ __forceinline__ void split_pos(float y, int &i, float &f) {
+    const float m = __fadd_rz(y, 12582912.0f);
+    i = __float_as_int(m) - 0x4B400000;
+    f = y - (m - 12582912.0f);
+}
+
+template <bool WEIGHTED, int SB, int DEG>
 __global__ void __launch_bounds__(256)
     bp_fan_kernel(const float *__restrict__ sino, float *__restrict__ img,
                   const float2 *__restrict__ view_cs, BpArgs a, int batch) {
     const int ix = blockIdx.x * kTile + threadIdx.x;
     const int iy0 = blockIdx.y * kTile + threadIdx.y;
-    const int b = blockIdx.z;
-    if (b >= batch) return;
-    float px = 0.f, py[kRowsPerThr];
+    const int b0 = blockIdx.z * SB;
+    float py[kRowsPerThr];
     bool in[kRowsPerThr];
     const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
-    px = (float)xd;
+    const float px = (float)xd;
     bool any = false;
 #pragma unroll
     for (int k = 0; k < kRowsPerThr; ++k) {
@@ -46,45 +75,58 @@ __global__ void __launch_bounds__(256)
         in[k] = ix < a.nx && iy < a.ny && (xd * xd + yd * yd <= a.fov_r2);
         any |= in[k];
     }
-    float acc[kRowsPerThr] = {0.f, 0.f, 0.f, 0.f};
+    float acc[SB][kRowsPerThr];
+#pragma unroll
+    for (int s = 0; s < SB; ++s)
+#pragma unroll
+        for (int k = 0; k < kRowsPerThr; ++k) acc[s][k] = 0.0f;
+    const size_t slice = (size_t)a.V * a.C;
     if (__syncthreads_or(any)) {
-        const float *sb = sino + (size_t)b * a.V * a.C;
-        const float fC = (float)a.C;
+        const float *sb[SB];
+#pragma unroll
+        for (int s = 0; s < SB; ++s) sb[s] = sino + (size_t)min(b0 + s, batch - 1) * slice;
         for (int v = 0; v < a.V; ++v) {
             const float2 cs = __ldg(view_cs + v);
-            const float *row = sb + (size_t)v * a.C;
+            const size_t ro = (size_t)v * a.C;
 #pragma unroll
             for (int k = 0; k < kRowsPerThr; ++k) {
-                const float U = a.R + px * cs.x + py[k] * cs.y;
-                const float t = -px * cs.y + py[k] * cs.x;
-                const float col = (atanf(t / U) - a.left) / a.dcol + a.shift;
-                if (in[k] && col > 0.0f && col < fC) {
-                    const float cb = col - 0.5f;
-                    const float fi = floorf(cb);
-                    const float f = cb - fi;
-                    const int i = (int)fi;
-                    const int i0 = max(i, 0), i1 = min(i + 1, a.C - 1);
-                    const float v0 = __ldg(row + i0), v1 = __ldg(row + i1);
-                    const float val = fmaf(f, v1 - v0, v0);
-                    if (WEIGHTED)
-                        acc[k] = fmaf(val, 1.0f / (U * U + t * t), acc[k]);
-                    else
-                        acc[k] += val;
+                const float U = fmaf(px, cs.x, fmaf(py[k], cs.y, a.R));
+                const float t = fmaf(py[k], cs.x, -px * cs.y);
+                const float rU = __fdividef(1.0f, U);
+                const float g = fov_atan<DEG>(t * rU, a.coef);
+                const float y = fmaf(g, a.inv_dcol, a.pos_off);
+                if (in[k] && y > 0.5f && y < a.fC + 0.5f) {
+                    int i;
+                    float f;
+                    split_pos(y, i, f);
+                    const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
+                    float wgt = 1.0f;
+                    if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));
+#pragma unroll
+                    for (int s = 0; s < SB; ++s) {
+                        const float v0 = __ldg(sb[s] + ro + i0), v1 = __ldg(sb[s] + ro + i1);
+                        const float val = fmaf(f, v1 - v0, v0);
+                        acc[s][k] = WEIGHTED ? fmaf(val, wgt, acc[s][k]) : acc[s][k] + val;
+                    }
                 }
             }
         }
     }
-    float *ib = img + (size_t)b * a.nx * a.ny;
 #pragma unroll
-    for (int k = 0; k < kRowsPerThr; ++k) {
-        const int iy = iy0 + 8 * k;
-        if (ix < a.nx && iy < a.ny) ib[(size_t)iy * a.nx + ix] = acc[k];
+    for (int s = 0; s < SB; ++s) {
+        if (b0 + s >= batch) break;
+        float *ib = img + (size_t)(b0 + s) * a.nx * a.ny;
+#pragma unroll
+        for (int k = 0; k < kRowsPerThr; ++k) {
+            const int iy = iy0 + 8 * k;
+            if (ix < a.nx && iy < a.ny) ib[(size_t)iy * a.nx + ix] = acc[s][k];
+        }
     }
 }
 
 // Transpose of bp_fan_kernel: each pixel-view scatters x * weight * (1-f, f)
 // onto the two clamped detector taps with global atomics.
-template <bool WEIGHTED>
+template <bool WEIGHTED, int DEG>
 __global__ void __launch_bounds__(256)
     bp_fan_transpose_kernel(const float *__restrict__ img, float *__restrict__ sino,
                             const float2 *__restrict__ view_cs, BpArgs a, int batch) {
@@ -108,24 +150,24 @@ __global__ void __launch_bounds__(256)
     }
     if (!__syncthreads_or(any)) return;
     float *sb = sino + (size_t)b * a.V * a.C;
-    const float fC = (float)a.C;
     for (int v = 0; v < a.V; ++v) {
         const float2 cs = __ldg(view_cs + v);
         float *row = sb + (size_t)v * a.C;
 #pragma unroll
         for (int k = 0; k < kRowsPerThr; ++k) {
             if (xv[k] == 0.0f) continue;
-            const float U = a.R + px * cs.x + py[k] * cs.y;
-            const float t = -px * cs.y + py[k] * cs.x;
-            const float col = (atanf(t / U) - a.left) / a.dcol + a.shift;
-            if (col > 0.0f && col < fC) {
-                const float cb = col - 0.5f;
-                const float fi = floorf(cb);
-                const float f = cb - fi;
-                const int i = (int)fi;
-                const int i0 = max(i, 0), i1 = min(i + 1, a.C - 1);
+            const float U = fmaf(px, cs.x, fmaf(py[k], cs.y, a.R));
+            const float t = fmaf(py[k], cs.x, -px * cs.y);
+            const float rU = __fdividef(1.0f, U);
+            const float g = fov_atan<DEG>(t * rU, a.coef);
+            const float y = fmaf(g, a.inv_dcol, a.pos_off);
+            if (y > 0.5f && y < a.fC + 0.5f) {
+                int i;
+                float f;
+                split_pos(y, i, f);
+                const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
                 float val = xv[k];
-                if (WEIGHTED) val *= 1.0f / (U * U + t * t);
+                if (WEIGHTED) val *= __fdividef(1.0f, fmaf(U, U, t * t));
                 atomicAdd(row + i0, val * (1.0f - f));
                 atomicAdd(row + i1, val * f);
             }
@@ -144,11 +186,37 @@ BpArgs make_args(const ct_plan *p) {
     a.dx = p->g.dx;
     a.dy = p->g.dy;
     a.R = p->g.sid;
-    a.left = p->g.left;
-    a.dcol = p->g.dcol;
-    a.shift = p->g.shift;
+    const double inv = 1.0 / (double)p->g.dcol;
+    a.inv_dcol = (float)inv;
+    a.pos_off = (float)((double)p->g.shift - (double)p->g.left * inv + 0.5);
+    a.fC = (float)a.C;
     a.fov_r2 = (double)p->g.rfov * (double)p->g.rfov;
+    for (int k = 0; k < 9; ++k) a.coef[k] = p->atan_coef[k];
     return a;
+}
+
+template <bool W, int SB>
+void launch_bp(int deg, dim3 grid, cudaStream_t s, const float *sp, float *ip, const float2 *vcs,
+               const BpArgs &a, int nb) {
+    dim3 block(kTile, 8, 1);
+    if (deg == 4)
+        bp_fan_kernel<W, SB, 4><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
+    else if (deg == 8)
+        bp_fan_kernel<W, SB, 8><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
+    else
+        bp_fan_kernel<W, SB, 0><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
+}
+
+template <bool W>
+void launch_bpt(int deg, dim3 grid, cudaStream_t s, const float *ip, float *sp, const float2 *vcs,
+                const BpArgs &a, int nb) {
+    dim3 block(kTile, 8, 1);
+    if (deg == 4)
+        bp_fan_transpose_kernel<W, 4><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+    else if (deg == 8)
+        bp_fan_transpose_kernel<W, 8><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+    else
+        bp_fan_transpose_kernel<W, 0><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
 }
 
 }  // namespace
@@ -158,16 +226,24 @@ int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weigh
     const BpArgs a = make_args(p);
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
     cudaStream_t s = (cudaStream_t)stream;
-    for (int b0 = 0; b0 < batch; b0 += 65535) {
-        const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
-        dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + kTile - 1) / kTile, nb);
-        dim3 block(kTile, 8, 1);
+    const int SB = batch >= 4 ? 4 : 1;
+    const int per_launch = 65535 * SB;
+    for (int b0 = 0; b0 < batch; b0 += per_launch) {
+        const int nb = batch - b0 < per_launch ? batch - b0 : per_launch;
+        dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + kTile - 1) / kTile, (nb + SB - 1) / SB);
         const float *sp = sino + (size_t)b0 * a.V * a.C;
         float *ip = img + (size_t)b0 * a.nx * a.ny;
-        if (weighted)
-            bp_fan_kernel<true><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
-        else
-            bp_fan_kernel<false><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
+        if (SB == 4) {
+            if (weighted)
+                launch_bp<true, 4>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
+            else
+                launch_bp<false, 4>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
+        } else {
+            if (weighted)
+                launch_bp<true, 1>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
+            else
+                launch_bp<false, 1>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
+        }
         ct_count_launch();
     }
     return (int)cudaGetLastError();
@@ -183,13 +259,12 @@ int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch,
     for (int b0 = 0; b0 < batch; b0 += 65535) {
         const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
         dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + kTile - 1) / kTile, nb);
-        dim3 block(kTile, 8, 1);
         const float *ip = img + (size_t)b0 * a.nx * a.ny;
         float *sp = sino + (size_t)b0 * a.V * a.C;
         if (weighted)
-            bp_fan_transpose_kernel<true><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+            launch_bpt<true>(p->atan_deg, grid, s, ip, sp, vcs, a, nb);
         else
-            bp_fan_transpose_kernel<false><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+            launch_bpt<false>(p->atan_deg, grid, s, ip, sp, vcs, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(kThreads)
         float acc[kRows];
         const float *ti = st + i + C - 1;  // ti[-j] = h[i - j]
         if (ODD_ONLY) {
-            const float h0 = ti[0];
+            const float h0 = st[C - 1];  // h[0]
 #pragma unroll
             for (int r = 0; r < kRows; ++r) acc[r] = h0 * sp[r * C + i];
             for (int j = (i & 1) ^ 1; j < C; j += 2) {

@@ -3,6 +3,7 @@
 // double-precision tables are identical on x86-64 and aarch64 hosts.
 #include <cmath>
 #include <cstring>
+#include <utility>
 
 #include "internal.h"
 
@@ -173,4 +174,79 @@ void ct_build_filter_taps(const ct_fan_geom *g, int window, ct_host_tables *t) {
         }
         t->taps[(size_t)(n + C - 1)] = static_cast<float>(h * scale);
     }
+}
+
+double ct_max_tan_gamma(const ct_fan_geom *g) {
+    const double r = g->rfov, R = g->sid;
+    return r / std::sqrt(R * R - r * r);
+}
+
+namespace {
+// Solves the (n x n, n <= 9) system A x = b by Gaussian elimination with
+// partial pivoting; A is row-major and overwritten.
+void solve_small(double *A, double *b, int n) {
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(A[r * n + c]) > std::fabs(A[piv * n + c])) piv = r;
+        if (piv != c) {
+            for (int k = 0; k < n; ++k) std::swap(A[c * n + k], A[piv * n + k]);
+            std::swap(b[c], b[piv]);
+        }
+        for (int r = c + 1; r < n; ++r) {
+            const double f = A[r * n + c] / A[c * n + c];
+            for (int k = c; k < n; ++k) A[r * n + k] -= f * A[c * n + k];
+            b[r] -= f * b[c];
+        }
+    }
+    for (int c = n - 1; c >= 0; --c) {
+        double s = b[c];
+        for (int k = c + 1; k < n; ++k) s -= A[c * n + k] * b[k];
+        b[c] = s / A[c * n + c];
+    }
+}
+}  // namespace
+
+// atan(z)/z is smooth and even, so it is interpolated as a polynomial in
+// s = z^2 on [0, zmax^2] at the deg+1 Chebyshev nodes (solved in the scaled
+// variable x = s/zmax^2 for conditioning), then checked on a dense grid.
+int ct_fit_atan(double zmax, float coef[9]) {
+    const double pi = 3.14159265358979323846;
+    for (int k = 0; k < 9; ++k) coef[k] = 0.0f;
+    if (!(zmax > 0.0) || zmax > 1.0) return 0;
+    const double smax = zmax * zmax;
+    const int degs[2] = {4, 8};
+    for (int deg : degs) {
+        const int n = deg + 1;
+        double A[81], b[9];
+        for (int i = 0; i < n; ++i) {
+            const double x = 0.5 * (1.0 - std::cos((2.0 * i + 1.0) * pi / (2.0 * n)));
+            const double s = x * smax, z = std::sqrt(s);
+            b[i] = s > 0.0 ? std::atan(z) / z : 1.0;
+            double xp = 1.0;
+            for (int k = 0; k < n; ++k) {
+                A[i * n + k] = xp;
+                xp *= x;
+            }
+        }
+        solve_small(A, b, n);
+        double c[9];
+        double scale = 1.0;
+        for (int k = 0; k < n; ++k) {
+            c[k] = b[k] / scale;  // coefficient of s^k
+            scale *= smax;
+        }
+        double err = 0.0;
+        for (int i = 0; i <= 4000; ++i) {
+            const double z = zmax * i / 4000.0, s = z * z;
+            double p = c[deg];
+            for (int k = deg - 1; k >= 0; --k) p = p * s + c[k];
+            err = std::fmax(err, std::fabs(z * p - std::atan(z)));
+        }
+        if (err <= 3e-8) {
+            for (int k = 0; k < n; ++k) coef[k] = static_cast<float>(c[k]);
+            return deg;
+        }
+    }
+    return 0;
 }

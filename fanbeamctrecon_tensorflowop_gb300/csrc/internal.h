@@ -35,6 +35,12 @@ ct_status ct_validate_geom(const ct_fan_geom *g);
 void ct_build_view_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
 void ct_build_ray_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
 void ct_build_filter_taps(const ct_fan_geom *g, int window, ct_host_tables *t);
+// Largest |t/U| = tan(gamma) over the FOV disc: rfov / sqrt(R^2 - rfov^2).
+double ct_max_tan_gamma(const ct_fan_geom *g);
+// Fits atan(z) = z * sum_k coef[k] (z^2)^k on |z| <= zmax (interpolation at
+// Chebyshev nodes in z^2); returns the degree used (4 or 8) or 0 when no
+// degree <= 8 reaches 3e-8 absolute error (callers then use atanf).
+int ct_fit_atan(double zmax, float coef[9]);
 
 struct ct_plan {
     ct_fan_geom g;
@@ -43,6 +49,8 @@ struct ct_plan {
     int filter_algo;                 // resolved ct_filter_algo (never AUTO)
     float fp_weight;                 // 0.125*dx (FP/transform.cu:144)
     float fov_r2;                    // rfov^2 (BP/transform.cu:116)
+    int atan_deg;                    // 4 or 8: polynomial atan on the FOV; 0: atanf
+    float atan_coef[9];
     double total_samples;
     int32_t max_nsamp;
     std::vector<float> h_view_cs;    // host copy of the view table

@@ -65,6 +65,15 @@ class FanPlan:
         except Exception:
             pass
 
+    @property
+    def total_samples(self) -> int:
+        """Ray samples of one FP slice (sum of floor(chord/0.125) over rays)."""
+        if getattr(self, "_total_samples", None) is None:
+            from .geometry import ray_table
+            _, ns = ray_table(self.param16, self.angles)
+            self._total_samples = int(ns.astype(np.int64).sum())
+        return self._total_samples
+
     # -- shapes -----------------------------------------------------------------
     @property
     def image_shape(self) -> tuple[int, int]:
