@@ -24,6 +24,7 @@ FILTER_AUTO = 0
 FILTER_DIRECT = 1
 FILTER_TOEPLITZ_TC = 2
 OP_FP, OP_FP_ADJOINT, OP_BP, OP_FBP, OP_FBP_ADJOINT, OP_FDK_BP, OP_BP_ADJOINT = range(7)
+FBP_STATIC_SCRATCH_FLOATS = 8 * 1024 * 1024  # CT_FBP_STATIC_SCRATCH_FLOATS
 
 
 class CtError(RuntimeError):
@@ -86,6 +87,7 @@ SIGNATURES = {
     "ct_fbp_fan": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_fbp_fan_adjoint": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_fdk_bp": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
+    "ct_fbp_fan_static_scratch": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan_adjoint": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_bp_fan": (_i, [_vp, _vp, _vp, _i, _vp]),

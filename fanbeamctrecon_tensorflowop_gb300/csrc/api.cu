@@ -123,6 +123,8 @@ ct_status filtered_bp(const ct_plan *p, const float *d_sino, float *d_img, int b
 
 void ct_count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+void ct_set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
 extern "C" {
 
 const char *ct_status_string(ct_status s) {

@@ -78,3 +78,5 @@ int plain_bp_fan(const ct_plan *p, const float *sino, float *img, int batch, voi
 
 // Launch accounting (api.cu).
 void ct_count_launch(uint64_t n = 1);
+// Sets the text ct_last_error() returns on this thread (api.cu).
+void ct_set_last_error(const char *msg);

@@ -224,6 +224,36 @@ ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_s
 ct_status ct_fdk_bp(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
                     void *d_work, size_t work_bytes, ct_stream stream);
 
+/* ---- filtered backprojection that allocates nothing ----------------------- */
+
+/* Capacity, in floats, of the fixed device array ct_fbp_fan_static_scratch
+ * uses: 8 Mi floats = 32 MiB, i.e. batch * n_views * n_cols <= 8,388,608
+ * (nine 984 x 888 sinograms per call). */
+#define CT_FBP_STATIC_SCRATCH_FLOATS (8u * 1024u * 1024u)
+
+/* Same result as ct_fbp_fan, for callers that cannot allocate device memory:
+ * plugins whose host framework owns all device memory and passes the plugin
+ * only its input and output buffers, and real-time pipelines that allow no
+ * device allocation after start-up (an allocation can synchronise the device
+ * and has no latency bound).  It calls no cudaMalloc, cudaMallocAsync,
+ * cudaFree or allocating library routine; the filtered sinogram lives in a
+ * fixed array of CT_FBP_STATIC_SCRATCH_FLOATS floats inside this library's
+ * device code, which every GPU that loads the library holds until the process
+ * exits.  The caller still passes the input and output buffers.
+ *   - batch * n_views * n_cols above the capacity returns CT_ERR_WORKSPACE
+ *     (ct_last_error says by how much); split the batch.
+ *   - The first call on each device looks up the array's device address with
+ *     that device current (cudaGetSymbolAddress) and caches it; make that
+ *     first call before capturing any stream into a CUDA graph.
+ *   - All calls on a device share the one array, which keeps the last call's
+ *     contents (each call overwrites all it reads, so nothing needs clearing).
+ *     Calls whose work overlaps on the GPU -- on different streams, or from
+ *     different host threads -- race on it; serialise them.
+ * No counterpart in the reference (its FBP malloc'ed and freed host and
+ * device buffers on every call). */
+ct_status ct_fbp_fan_static_scratch(const ct_plan *plan, const float *d_sino, float *d_img,
+                                    int batch, ct_stream stream);
+
 /* ---- the plain per-view launch loop (comparison baseline) ----------------- */
 
 /* The reference's execution structure on the same GPU: for each slice and
