@@ -79,6 +79,8 @@ ct_status check_call(const ct_plan *p, const void *in, const void *out, int batc
 
 size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
     switch (op) {
+        case CT_OP_FP:
+            return ctk::fp_fan_work_bytes(p, batch);
         case CT_OP_FBP:
         case CT_OP_FBP_ADJOINT:
         case CT_OP_FDK_BP:
@@ -239,13 +241,16 @@ ct_status ct_workspace_size(const ct_plan *plan, ct_op op, int batch, size_t *by
 
 ct_status ct_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
                     void *d_work, size_t work_bytes, ct_stream stream) {
-    (void)d_work;
-    (void)work_bytes;
     ct_status st = check_call(plan, d_img, d_sino, batch);
     if (st != CT_OK || batch == 0) return st;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
-    return launch_status(ctk::fp_fan(plan, d_img, d_sino, batch, stream), "ct_fp_fan");
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, op_workspace(plan, CT_OP_FP, batch), stream);
+    if (st != CT_OK) return st;
+    return launch_status(
+        ctk::fp_fan(plan, d_img, d_sino, batch, w.ptr, stream),
+        "ct_fp_fan");
 }
 
 ct_status ct_fp_fan_adjoint(const ct_plan *plan, const float *d_sino, float *d_img, int batch,

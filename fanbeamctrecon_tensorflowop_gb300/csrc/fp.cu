@@ -6,6 +6,11 @@
 // samples in closed form (cellwalk.cuh), so the image is read once per cell
 // instead of four times per sample; SB slices share one walk.  Output:
 // p = 0.125*dx * sum_k bilinear_clamp(img, start + k*step), k < n.
+// The lanes of a warp are adjacent rays of one view.  A ray running mostly
+// along x reads a transposed copy of the image (built per launch in the
+// workspace), so that for every view the lanes' taps lie along memory rows
+// and a warp's gather touches one or two cache lines per tap, not one line
+// per lane.
 //
 // Transpose: one block per 32x32 image tile and slice keeps the tile in
 // shared memory.  For every view it takes the rays that can reach the tile,
@@ -14,6 +19,7 @@
 // tile owns.  Every pixel is written exactly once; there are no global
 // atomics.
 #include <cfloat>
+#include <climits>
 
 #include "cellwalk.cuh"
 
@@ -21,48 +27,155 @@ namespace ctk {
 namespace {
 
 constexpr int kFpThreads = 256;
+constexpr int kFpChunk = 64;  // slices per quad-workspace chunk
+
+// Quad images: for every bilinear cell (cu, cv) of the walked layout, the
+// four clamp-to-edge taps (cu,cv), (cu+1,cv), (cu,cv+1), (cu+1,cv+1) as one
+// float4, so a cell's gather is a single 16-byte load.  Samples lie inside
+// the FOV circle of radius nx/2 texels, so cells run over [-1, nx-1] in both
+// axes of both layouts; quad (qi, qj) holds cell (qi-1, qj-1) and a layout
+// is (nx+1)^2 quads.  Layout 0 walks (u, v) = (x, y); layout 1 walks the
+// transposed image, (u, v) = (y, x).
+__global__ void __launch_bounds__(256)
+    build_quads_kernel(const float *__restrict__ img, float4 *__restrict__ quads, int nx, int ny) {
+    const int Q = nx + 1;
+    const int qi = blockIdx.x * 32 + threadIdx.x, qj = blockIdx.y * 8 + threadIdx.y;
+    if (qi >= Q || qj >= Q) return;
+    const int layout = blockIdx.z & 1, b = blockIdx.z >> 1;
+    const float *im = img + (size_t)b * nx * ny;
+    const int cu = qi - 1, cv = qj - 1;
+    // tap (du, dv) of the cell is image pixel x = cu+du, y = cv+dv (layout 0)
+    // or x = cv+dv, y = cu+du (layout 1), clamped to the image
+    float4 t;
+    float *tv = &t.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int du = k & 1, dv = k >> 1;
+        int x = layout ? cv + dv : cu + du;
+        int y = layout ? cu + du : cv + dv;
+        x = min(max(x, 0), nx - 1);
+        y = min(max(y, 0), ny - 1);
+        tv[k] = __ldg(im + (size_t)y * nx + x);
+    }
+    quads[((size_t)b * 2 + layout) * Q * Q + (size_t)qj * Q + qi] = t;
+}
 
 template <int SB>
-__global__ void __launch_bounds__(kFpThreads)
-    fp_fan_kernel(const float *__restrict__ img, float *__restrict__ sino,
-                  const float4 *__restrict__ ray, const int *__restrict__ nsamp, int n_rays,
-                  int nx, int ny, float w, int batch, int max_iter) {
-    const int r = blockIdx.x * kFpThreads + threadIdx.x;
-    if (r >= n_rays) return;
-    const int b0 = blockIdx.y * SB;
-    const int n = __ldg(nsamp + r);
-    const size_t plane = (size_t)nx * ny;
+struct Taps {
+    const float4 *q;  // this warp's layout of slice b0; slice s adds s * stride
+    size_t stride;    // quads between consecutive slices
+    int Q;            // quads per row (nx + 1)
     float acc[SB];
+    __device__ __forceinline__ void add(const CellWeights &cw, int cu, int cv) {
+        const int qi = min(max(cu + 1, 0), Q - 1), qj = min(max(cv + 1, 0), Q - 1);
+        const float4 *p = q + (size_t)qj * Q + qi;
 #pragma unroll
-    for (int s = 0; s < SB; ++s) acc[s] = 0.0f;
-    if (n > 0) {
-        const float4 q = __ldg(ray + r);
-        const RaySeg seg{q.x - 0.5f, q.y - 0.5f, q.z, q.w};
-        const float *im[SB];
-#pragma unroll
-        for (int s = 0; s < SB; ++s) im[s] = img + (size_t)min(b0 + s, batch - 1) * plane;
-        walk_cells(seg, 0.0f, (float)n, max_iter,
-                   [&](int cu, int cv, float cnt, float a, float b) {
-                       const CellWeights cw = cell_weights(cnt, a, b, seg.su, seg.sv);
-                       // clamp-to-edge taps (for nx != ny the FOV circle, of
-                       // radius nx/2 in both axes, can leave the image rows)
-                       const int i0 = min(max(cu, 0), nx - 1), i1 = min(max(cu + 1, 0), nx - 1);
-                       const int r0 = min(max(cv, 0), ny - 1) * nx;
-                       const int r1 = min(max(cv + 1, 0), ny - 1) * nx;
-#pragma unroll
-                       for (int s = 0; s < SB; ++s) {
-                           const float *p = im[s];
-                           float v = cw.w00 * __ldg(p + r0 + i0);
-                           v = fmaf(cw.w10, __ldg(p + r0 + i1), v);
-                           v = fmaf(cw.w01, __ldg(p + r1 + i0), v);
-                           v = fmaf(cw.w11, __ldg(p + r1 + i1), v);
-                           acc[s] += v;
-                       }
-                   });
+        for (int s = 0; s < SB; ++s) {
+            const float4 t = __ldg(p + s * stride);
+            float v = cw.w00 * t.x;
+            v = fmaf(cw.w10, t.y, v);
+            v = fmaf(cw.w01, t.z, v);
+            v = fmaf(cw.w11, t.w, v);
+            acc[s] += v;
+        }
     }
+};
+
+// One warp = 32 consecutive channels of one view (warps never straddle views;
+// wpv warps per view).  The warp votes its layout (transposed when most rays
+// run along x) and its row direction, then steps through the rows of that
+// layout in lockstep: in each row every lane sums the (one to three) cells its
+// ray crosses there.  Lanes therefore gather from the same one or two rows at
+// a time, whatever depth their rays entered the FOV at.  A lane whose ray
+// runs against the warp's direction (possible only at a layout boundary)
+// walks on its own afterwards.
+template <int SB>
+__global__ void __launch_bounds__(kFpThreads)
+    fp_fan_kernel(const float4 *__restrict__ quads, float *__restrict__ sino,
+                  const float4 *__restrict__ ray, const int *__restrict__ nsamp, int V, int C,
+                  int wpv, int nx, float w, int batch, int max_iter) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (kFpThreads / 32) + (threadIdx.x >> 5);
+    if (gw >= V * wpv) return;  // warp-uniform
+    const int v = gw / wpv;
+    const int c = (gw - v * wpv) * 32 + lane;
+    const bool has_c = c < C;
+    const int r = v * C + (has_c ? c : C - 1);
+    const int b0 = blockIdx.y * SB;
+    const int n = has_c ? __ldg(nsamp + r) : 0;
+    const bool valid = n > 0;
+    const float4 q = valid ? __ldg(ray + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+
+    const unsigned vm = __ballot_sync(FULL, valid);
+    const unsigned xm = __ballot_sync(FULL, valid && fabsf(q.z) > fabsf(q.w));
+    const bool along_x = 2 * __popc(xm) > __popc(vm);
+    const RaySeg seg = along_x ? RaySeg{q.y - 0.5f, q.x - 0.5f, q.w, q.z}
+                               : RaySeg{q.x - 0.5f, q.y - 0.5f, q.z, q.w};
+    Taps<SB> tp;
+    tp.Q = nx + 1;
+    const size_t lsz = (size_t)tp.Q * tp.Q;
+    tp.stride = 2 * lsz;
+    // slices beyond the batch read the last slice's quads (results dropped)
+    tp.q = quads + (size_t)b0 * tp.stride + (along_x ? lsz : 0);
 #pragma unroll
-    for (int s = 0; s < SB; ++s)
-        if (b0 + s < batch) sino[(size_t)(b0 + s) * n_rays + r] = acc[s] * w;
+    for (int s = 0; s < SB; ++s) tp.acc[s] = 0.0f;
+    const unsigned pm = __ballot_sync(FULL, valid && seg.sv > 0.0f);
+    const int dir = 2 * __popc(pm) >= __popc(vm) ? 1 : -1;
+    const bool synced = valid && (dir > 0 ? seg.sv > 0.0f : seg.sv < 0.0f);
+    const float nf = (float)n;
+    // rows of the first and last sample, one row of slack on each side
+    const int jf = (int)floorf(seg.v0);
+    const int jl = (int)floorf(fmaf(seg.sv, nf - 1.0f, seg.v0));
+    int J0, J1;
+    if (dir > 0) {
+        J0 = __reduce_min_sync(FULL, synced ? jf : INT_MAX) - 1;
+        J1 = __reduce_max_sync(FULL, synced ? jl : INT_MIN) + 1;
+    } else {
+        J0 = __reduce_max_sync(FULL, synced ? jf : INT_MIN) + 1;
+        J1 = __reduce_min_sync(FULL, synced ? jl : INT_MAX) - 1;
+    }
+    if (__any_sync(FULL, synced)) {
+        const float INF = __int_as_float(0x7f800000);
+        const float iu = seg.su != 0.0f ? 1.0f / seg.su : 0.0f;
+        const float iv = synced ? 1.0f / seg.sv : 0.0f;
+        const float du = seg.su >= 0.0f ? 1.0f : -1.0f;
+        const int rows = (J1 - J0) * dir + 1;
+        for (int it = 0; it < rows; ++it) {
+            const int j = J0 + it * dir;
+            if (!synced) continue;
+            const float tA = ((float)j - seg.v0) * iv, tB = ((float)(j + 1) - seg.v0) * iv;
+            const float ka = fmaxf(0.0f, ceilf(fminf(tA, tB)));
+            const float kb = fminf(nf, ceilf(fmaxf(tA, tB)));
+            if (!(ka < kb)) continue;
+            float cu = floorf(fmaf(seg.su, ka, seg.u0));
+            float bu = seg.su >= 0.0f ? cu + 1.0f : cu;
+            float k = ka;
+            for (int t = 0; t < 8 && k < kb; ++t) {
+                const float tu = seg.su != 0.0f ? (bu - seg.u0) * iu : INF;
+                const float ke = fminf(kb, ceilf(tu));
+                const float cnt = ke - k;
+                if (cnt > 0.0f) {
+                    const float a = fmaf(seg.su, k, seg.u0) - cu;
+                    const float b = fmaf(seg.sv, k, seg.v0) - (float)j;
+                    tp.add(cell_weights(cnt, a, b, seg.su, seg.sv), (int)cu, j);
+                    k = ke;
+                }
+                cu += du;
+                bu += du;
+            }
+        }
+    }
+    if (valid && !synced) {
+        walk_cells(seg, 0.0f, nf, max_iter, [&](int cu, int cv, float cnt, float a, float b) {
+            tp.add(cell_weights(cnt, a, b, seg.su, seg.sv), cu, cv);
+        });
+    }
+    if (has_c) {
+#pragma unroll
+        for (int s = 0; s < SB; ++s)
+            if (b0 + s < batch) sino[((size_t)(b0 + s) * V + v) * C + c] = tp.acc[s] * w;
+    }
 }
 
 // ---- transpose ----------------------------------------------------------------
@@ -188,26 +301,53 @@ __global__ void __launch_bounds__(kAdjThreads)
 
 }  // namespace
 
-int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *stream) {
-    const int n_rays = p->g.n_views * p->g.n_cols;
-    const int bx = (n_rays + kFpThreads - 1) / kFpThreads;
-    const int max_iter = 2 * (p->g.nx > p->g.ny ? p->g.nx : p->g.ny) + 8;
+size_t fp_fan_work_bytes(const ct_plan *p, int batch) {
+    const size_t q = (size_t)(p->g.nx + 1) * (p->g.nx + 1);
+    const size_t chunk = batch < kFpChunk ? (size_t)batch : (size_t)kFpChunk;
+    return chunk * 2 * q * sizeof(float4);
+}
+
+int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *work,
+           void *stream) {
+    const int V = p->g.n_views, C = p->g.n_cols;
+    const int nx = p->g.nx, ny = p->g.ny;
+    const int max_iter = 2 * (nx > ny ? nx : ny) + 8;
+    const size_t plane = (size_t)nx * ny;
+    const size_t n_rays = (size_t)V * C;
     const float4 *ray = reinterpret_cast<const float4 *>(p->d_ray);
+    float4 *quads = static_cast<float4 *>(work);
     cudaStream_t s = (cudaStream_t)stream;
-    // four slices per walk while at least four remain, then one at a time
-    const int b4 = batch / 4 * 4;
-    for (int b0 = 0; b0 < b4; b0 += 4 * 65535) {
-        const int nb = b4 - b0 < 4 * 65535 ? b4 - b0 : 4 * 65535;
-        fp_fan_kernel<4><<<dim3(bx, nb / 4), kFpThreads, 0, s>>>(
-            img + (size_t)b0 * p->g.nx * p->g.ny, sino + (size_t)b0 * n_rays, ray, p->d_nsamp,
-            n_rays, p->g.nx, p->g.ny, p->fp_weight, nb, max_iter);
+    const int wpv = (C + 31) / 32;
+    const int blocks = (V * wpv + kFpThreads / 32 - 1) / (kFpThreads / 32);
+    const int Q = nx + 1;
+    // chunks of at most kFpChunk slices share the quad workspace
+    for (int c0 = 0; c0 < batch; c0 += kFpChunk) {
+        const int nb = batch - c0 < kFpChunk ? batch - c0 : kFpChunk;
+        build_quads_kernel<<<dim3((Q + 31) / 32, (Q + 7) / 8, 2 * nb), dim3(32, 8), 0, s>>>(
+            img + (size_t)c0 * plane, quads, nx, ny);
         ct_count_launch();
-    }
-    if (batch > b4) {
-        fp_fan_kernel<1><<<dim3(bx, batch - b4), kFpThreads, 0, s>>>(
-            img + (size_t)b4 * p->g.nx * p->g.ny, sino + (size_t)b4 * n_rays, ray, p->d_nsamp,
-            n_rays, p->g.nx, p->g.ny, p->fp_weight, batch - b4, max_iter);
-        ct_count_launch();
+        float *out = sino + (size_t)c0 * n_rays;
+        int b = 0;
+        if (nb >= 8) {
+            const int n8 = nb / 8 * 8;
+            fp_fan_kernel<8><<<dim3(blocks, n8 / 8), kFpThreads, 0, s>>>(
+                quads, out, ray, p->d_nsamp, V, C, wpv, nx, p->fp_weight, n8, max_iter);
+            ct_count_launch();
+            b = n8;
+        }
+        if (nb - b >= 4) {
+            fp_fan_kernel<4><<<dim3(blocks, 1), kFpThreads, 0, s>>>(
+                quads + (size_t)b * 2 * Q * Q, out + (size_t)b * n_rays, ray, p->d_nsamp, V, C,
+                wpv, nx, p->fp_weight, 4, max_iter);
+            ct_count_launch();
+            b += 4;
+        }
+        if (nb > b) {
+            fp_fan_kernel<1><<<dim3(blocks, nb - b), kFpThreads, 0, s>>>(
+                quads + (size_t)b * 2 * Q * Q, out + (size_t)b * n_rays, ray, p->d_nsamp, V, C,
+                wpv, nx, p->fp_weight, nb - b, max_iter);
+            ct_count_launch();
+        }
     }
     return (int)cudaGetLastError();
 }

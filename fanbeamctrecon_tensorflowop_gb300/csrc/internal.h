@@ -63,7 +63,10 @@ struct ct_plan {
 
 // Kernel launchers (defined in the .cu files).  Each returns the launch error.
 namespace ctk {
-int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *stream);
+// work: fp_fan_work_bytes(p, batch) bytes (quad images of up to 64 slices)
+int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *work,
+           void *stream);
+size_t fp_fan_work_bytes(const ct_plan *p, int batch);
 int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
 // mode 0: unweighted BP, 1: 1/(U^2+t^2)-weighted (FBP / FDK 2-D)
 int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weighted, void *stream);
