@@ -6,12 +6,12 @@ Python interface (``utils``, ``config``).
 """
 from . import _lib
 from .geometry import angle, decode, fan_param16, param_set
-from .ops import FanPlan, clear_plan_cache, get_plan
-from .autograd import (back_project, fdk_back_project, filtered_back_project, forward_project,
-                       forward_project_adjoint)
+from .ops import ConePlan, FanPlan, clear_plan_cache, get_plan
+from .autograd import (back_project, fdk_back_project, fdk_cone, filtered_back_project,
+                       forward_project, forward_project_adjoint)
 
 __all__ = [
-    "FanPlan", "get_plan", "clear_plan_cache", "angle", "param_set", "decode", "fan_param16",
+    "FanPlan", "ConePlan", "fdk_cone", "get_plan", "clear_plan_cache", "angle", "param_set", "decode", "fan_param16",
     "forward_project", "forward_project_adjoint", "back_project", "filtered_back_project",
     "fdk_back_project",
 ]

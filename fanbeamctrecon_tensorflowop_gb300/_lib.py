@@ -23,7 +23,8 @@ WINDOW_SHEPP_LOGAN = 1
 FILTER_AUTO = 0
 FILTER_DIRECT = 1
 FILTER_TOEPLITZ_TC = 2
-OP_FP, OP_FP_ADJOINT, OP_BP, OP_FBP, OP_FBP_ADJOINT, OP_FDK_BP, OP_BP_ADJOINT = range(7)
+(OP_FP, OP_FP_ADJOINT, OP_BP, OP_FBP, OP_FBP_ADJOINT, OP_FDK_BP, OP_BP_ADJOINT, OP_FP_CONE,
+ OP_FDK_CONE, OP_FDK_CONE_ADJOINT) = range(10)
 FBP_STATIC_SCRATCH_FLOATS = 8 * 1024 * 1024  # CT_FBP_STATIC_SCRATCH_FLOATS
 
 
@@ -76,6 +77,8 @@ SIGNATURES = {
     "ct_fp_ray_table": (_i, [_P(CtFanGeom), _P(ctypes.c_float), _i, _P(ctypes.c_float),
                             _P(ctypes.c_int32)]),
     "ct_plan_create": (_i, [_P(CtFanGeom), _P(ctypes.c_float), _i, _P(CtPlanOpts), _P(_vp)]),
+    "ct_plan_create_cone": (_i, [_P(CtFanGeom), _i, _i, _P(ctypes.c_float), _i, _P(CtPlanOpts),
+                                 _P(_vp)]),
     "ct_plan_destroy": (_i, [_vp]),
     "ct_plan_geom": (_i, [_vp, _P(CtFanGeom)]),
     "ct_workspace_size": (_i, [_vp, _i, _i, _P(_sz)]),
@@ -87,6 +90,10 @@ SIGNATURES = {
     "ct_fbp_fan": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_fbp_fan_adjoint": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_fdk_bp": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
+    "ct_cone_bp": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "ct_fdk_cone": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
+    "ct_fdk_cone_adjoint": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
+    "ct_fp_cone": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_fbp_fan_static_scratch": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan_adjoint": (_i, [_vp, _vp, _vp, _i, _vp]),

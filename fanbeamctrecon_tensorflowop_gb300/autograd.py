@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import torch
 
-from .ops import FanPlan
+from .ops import ConePlan, FanPlan
 
 
 class _ForwardProjection(torch.autograd.Function):
@@ -108,3 +108,23 @@ def filtered_back_project(sino: torch.Tensor, plan: FanPlan) -> torch.Tensor:
 def fdk_back_project(sino: torch.Tensor, plan: FanPlan) -> torch.Tensor:
     """Differentiable reference FDK op; backward is its transpose."""
     return _FDKBackProjection.apply(sino, plan)
+
+
+class _FDKCone(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, proj: torch.Tensor, plan: ConePlan) -> torch.Tensor:
+        ctx.plan = plan
+        ctx.squeeze = proj.dim() == 3
+        out = plan.fdk(proj)
+        return out[0] if ctx.squeeze else out
+
+    @staticmethod
+    def backward(ctx, g: torch.Tensor):
+        gp = ctx.plan.fdk_adjoint(g.contiguous())
+        return (gp[0] if ctx.squeeze else gp), None
+
+
+def fdk_cone(proj: torch.Tensor, plan: ConePlan) -> torch.Tensor:
+    """Differentiable cone-beam FDK; backward is its exact transpose
+    (CB_EA transpose, then the filter)."""
+    return _FDKCone.apply(proj, plan)

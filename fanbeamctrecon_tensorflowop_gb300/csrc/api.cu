@@ -77,8 +77,17 @@ ct_status check_call(const ct_plan *p, const void *in, const void *out, int batc
     return CT_OK;
 }
 
+size_t proj_bytes(const ct_plan *p, int batch) {
+    return sizeof(float) * (size_t)batch * p->g.n_views * p->n_rows * p->g.n_cols;
+}
+
 size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
     switch (op) {
+        case CT_OP_FP_CONE:
+            return ctk::cone_fp_work_bytes(p, batch);
+        case CT_OP_FDK_CONE:
+        case CT_OP_FDK_CONE_ADJOINT:
+            return proj_bytes(p, batch);
         case CT_OP_FP:
             return ctk::fp_fan_work_bytes(p, batch);
         case CT_OP_FBP:
@@ -96,6 +105,7 @@ void free_plan(ct_plan *p) {
     cudaFree(p->d_ray);
     cudaFree(p->d_nsamp);
     cudaFree(p->d_taps);
+    cudaFree(p->d_chan_s);
     delete p;
 }
 
@@ -166,12 +176,16 @@ ct_status ct_fp_ray_table(const ct_fan_geom *geom, const float *angles, int n_an
     return CT_OK;
 }
 
-ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_angles,
-                         const ct_plan_opts *opts, ct_plan **out) {
+static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const float *angles,
+                             int n_angles, const ct_plan_opts *opts, ct_plan **out) {
     if (!geom || !angles || !out) return CT_ERR_NULL_POINTER;
     *out = nullptr;
     ct_status st = ct_validate_geom(geom);
     if (st != CT_OK) return st;
+    if (n_rows < 1 || nz < 1) return CT_ERR_INVALID_ARGUMENT;
+    if ((int64_t)geom->n_views * n_rows * geom->n_cols >= (int64_t)1 << 31 ||
+        (int64_t)nz * geom->nx * geom->ny >= (int64_t)1 << 31)
+        return CT_ERR_INVALID_ARGUMENT;
     if (n_angles != geom->n_views) return CT_ERR_INVALID_ARGUMENT;
     for (int v = 0; v < n_angles; ++v)
         if (!std::isfinite(angles[v])) return CT_ERR_INVALID_ARGUMENT;
@@ -192,6 +206,7 @@ ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_ang
     ct_build_view_table(geom, angles, &t);
     ct_build_ray_table(geom, angles, &t);
     ct_build_filter_taps(geom, o.filter_window, &t);
+    ct_build_channel_table(geom, &t);
 
     ct_plan *p = new (std::nothrow) ct_plan();
     if (!p) return CT_ERR_ALLOC;
@@ -201,6 +216,8 @@ ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_ang
     p->fp_weight = (float)(CT_FP_STEP * (double)geom->dx);
     p->fov_r2 = geom->rfov * geom->rfov;
     p->atan_deg = ct_fit_atan(1.02 * ct_max_tan_gamma(geom), p->atan_coef);
+    p->n_rows = n_rows;
+    p->nz = nz;
     p->total_samples = t.total_samples;
     p->max_nsamp = t.max_nsamp;
     p->h_view_cs = t.view_cs;
@@ -211,12 +228,26 @@ ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_ang
     }
     if ((st = upload(&p->d_view_cs, t.view_cs)) != CT_OK ||
         (st = upload(&p->d_ray, t.ray)) != CT_OK || (st = upload(&p->d_nsamp, t.nsamp)) != CT_OK ||
-        (st = upload(&p->d_taps, t.taps)) != CT_OK) {
+        (st = upload(&p->d_taps, t.taps)) != CT_OK ||
+        (st = upload(&p->d_chan_s, t.chan_s)) != CT_OK) {
         free_plan(p);
         return st;
     }
     *out = p;
     return CT_OK;
+}
+
+ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_angles,
+                         const ct_plan_opts *opts, ct_plan **out) {
+    return plan_create(geom, 1, 1, angles, n_angles, opts, out);
+}
+
+ct_status ct_plan_create_cone(const ct_fan_geom *geom, int n_rows, int nz, const float *angles,
+                              int n_angles, const ct_plan_opts *opts, ct_plan **out) {
+    if (!geom) return CT_ERR_NULL_POINTER;
+    if (!(geom->drow > 0.0f) || !(geom->dz > 0.0f) || !(geom->sdd > geom->sid))
+        return CT_ERR_INVALID_ARGUMENT;
+    return plan_create(geom, n_rows, nz, angles, n_angles, opts, out);
 }
 
 ct_status ct_plan_destroy(ct_plan *plan) {
@@ -234,7 +265,7 @@ ct_status ct_plan_geom(const ct_plan *plan, ct_fan_geom *out) {
 
 ct_status ct_workspace_size(const ct_plan *plan, ct_op op, int batch, size_t *bytes) {
     if (!plan || !bytes) return CT_ERR_NULL_POINTER;
-    if (batch < 0 || op < CT_OP_FP || op > CT_OP_BP_ADJOINT) return CT_ERR_INVALID_ARGUMENT;
+    if (batch < 0 || op < CT_OP_FP || op > CT_OP_FDK_CONE_ADJOINT) return CT_ERR_INVALID_ARGUMENT;
     *bytes = op_workspace(plan, op, batch);
     return CT_OK;
 }
@@ -334,6 +365,65 @@ ct_status ct_fdk_bp(const ct_plan *plan, const float *d_sino, float *d_img, int 
     // every row index to row 0, so CB_EA reduces to the weighted fan BP with
     // detector shift.
     return filtered_bp(plan, d_sino, d_img, batch, d_work, work_bytes, stream, "ct_fdk_bp");
+}
+
+ct_status ct_cone_bp(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,
+                     ct_stream stream) {
+    ct_status st = check_call(plan, d_proj, d_vol, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::cone_bp(plan, d_proj, d_vol, batch, stream), "ct_cone_bp");
+}
+
+ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,
+                      void *d_work, size_t work_bytes, ct_stream stream) {
+    ct_status st = check_call(plan, d_proj, d_vol, batch);
+    if (st != CT_OK || batch == 0) return st;
+    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, proj_bytes(plan, batch), stream);
+    if (st != CT_OK) return st;
+    float *filt = static_cast<float *>(w.ptr);
+    st = launch_status(
+        ctk::ramp_filter(plan, d_proj, filt, batch * plan->g.n_views * plan->n_rows, stream),
+        "ct_fdk_cone");
+    if (st != CT_OK) return st;
+    return launch_status(ctk::cone_bp(plan, filt, d_vol, batch, stream), "ct_fdk_cone");
+}
+
+ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_proj, int batch,
+                              void *d_work, size_t work_bytes, ct_stream stream) {
+    ct_status st = check_call(plan, d_vol, d_proj, batch);
+    if (st != CT_OK || batch == 0) return st;
+    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (sizeof(float) * 16 * (size_t)plan->g.n_cols > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, proj_bytes(plan, batch), stream);
+    if (st != CT_OK) return st;
+    float *tmp = static_cast<float *>(w.ptr);
+    st = launch_status(ctk::cone_bp_transpose(plan, d_vol, tmp, batch, stream),
+                       "ct_fdk_cone_adjoint");
+    if (st != CT_OK) return st;
+    return launch_status(
+        ctk::ramp_filter(plan, tmp, d_proj, batch * plan->g.n_views * plan->n_rows, stream),
+        "ct_fdk_cone_adjoint");
+}
+
+ct_status ct_fp_cone(const ct_plan *plan, const float *d_vol, float *d_proj, int batch,
+                     void *d_work, size_t work_bytes, ct_stream stream) {
+    ct_status st = check_call(plan, d_vol, d_proj, batch);
+    if (st != CT_OK || batch == 0) return st;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, ctk::cone_fp_work_bytes(plan, batch), stream);
+    if (st != CT_OK) return st;
+    return launch_status(ctk::cone_fp(plan, d_vol, d_proj, batch, w.ptr, stream), "ct_fp_cone");
 }
 
 ct_status ct_plain_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,

@@ -1,0 +1,512 @@
+// Cone-beam operators: the reference's CB_EA backprojection for nz slices and
+// n_rows detector rows (FDK), its transpose (the FDK adjoint), and a cone-beam
+// forward projector.
+//
+// Volumes are [B][nz][ny][nx]; projections [B][V][n_rows][C], the view layout
+// the reference's FDK filter walks (FDK/GPURecon_GPU.cu:211).  Voxel centres
+// are x = xmin + dx(i+1/2), y likewise, z = zmin + dz(k+1/2) with
+// zmin = -dz*nz/2 (FDK/FBP.cc:86); the source orbits at z = 0
+// (FDK/GPURecon_GPU.cu:226).
+#include <cfloat>
+#include <climits>
+
+#include "cellwalk.cuh"
+
+namespace ctk {
+namespace {
+
+constexpr int kThreads = 256;
+
+struct ConeArgs {
+    int V, C, nx, ny, nz, n_rows;
+    float xmin, ymin, dx, dy, zmin, dz;
+    float R, D;
+    float inv_dcol, pos_off, fC;  // column coordinate y = atan*inv_dcol + pos_off = col + 1/2
+    float row_scale;              // D / drow
+    float row_off;                // -det_bottom / drow + 1/2: row + 1/2 = z*row_scale/U + row_off
+    double fov_r2;
+    float coef[9];
+    int atan_deg;
+};
+
+template <int DEG>
+__device__ __forceinline__ float cone_atan(float z, const ConeArgs &a) {
+    if constexpr (DEG == 0) {
+        return atanf(z);
+    } else {
+        const float s = z * z;
+        float p = a.coef[DEG];
+#pragma unroll
+        for (int k = DEG - 1; k >= 0; --k) p = fmaf(p, s, a.coef[k]);
+        return z * p;
+    }
+}
+
+// y >= 0: i = trunc(y), f = frac(y) without conversion instructions.
+__device__ __forceinline__ void split_pos(float y, int &i, float &f) {
+    const float m = __fadd_rz(y, 12582912.0f);
+    i = __float_as_int(m) - 0x4B400000;
+    f = y - (m - 12582912.0f);
+}
+
+// ---- CB_EA backprojection ----------------------------------------------------
+// Thread = one (x, y) pixel and ZC consecutive z slices; block = 32 x 8 pixels.
+// Per view the column, the 1/(U^2+t^2) weight and the row slope are computed
+// once; each slice then needs one row coordinate and a bilinear (col, row)
+// sample of the view (FDK/GPURecon_GPU.cu:33-47).
+template <int ZC, int DEG>
+__global__ void __launch_bounds__(kThreads)
+    cone_bp_kernel(const float *__restrict__ proj, float *__restrict__ vol,
+                   const float2 *__restrict__ view_cs, ConeArgs a, int batch) {
+    const int ix = blockIdx.x * 32 + threadIdx.x;
+    const int iy = blockIdx.y * 8 + threadIdx.y;
+    const int zgroups = (a.nz + ZC - 1) / ZC;
+    const int b = blockIdx.z / zgroups;
+    const int k0 = (blockIdx.z - b * zgroups) * ZC;
+    const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
+    const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
+    const bool in = b < batch && ix < a.nx && iy < a.ny && (xd * xd + yd * yd <= a.fov_r2);
+    const float px = (float)xd, py = (float)yd;
+    float acc[ZC];
+#pragma unroll
+    for (int k = 0; k < ZC; ++k) acc[k] = 0.0f;
+    const size_t pview = (size_t)a.n_rows * a.C;
+    if (__syncthreads_or(in) && in) {
+        const float *pb = proj + (size_t)b * a.V * pview;
+        const float z0 = a.zmin + a.dz * ((float)k0 + 0.5f);
+        const float rmax = (float)a.n_rows;
+        for (int v = 0; v < a.V; ++v) {
+            const float2 cs = __ldg(view_cs + v);
+            const float U = fmaf(px, cs.x, fmaf(py, cs.y, a.R));
+            const float t = fmaf(py, cs.x, -px * cs.y);
+            const float rU = __fdividef(1.0f, U);
+            const float y = fmaf(cone_atan<DEG>(t * rU, a), a.inv_dcol, a.pos_off);
+            if (!(y > 0.5f && y < a.fC + 0.5f)) continue;
+            int ic;
+            float f;
+            split_pos(y, ic, f);
+            const int i0 = max(ic - 1, 0), i1 = min(ic, a.C - 1);
+            const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
+            const float *pv = pb + (size_t)v * pview;
+            // row + 1/2 of slice k0 + kk: rr0 + kk * drr
+            const float slope = a.row_scale * rU;
+            const float rr0 = fmaf(z0, slope, a.row_off);
+            const float drr = a.dz * slope;
+#pragma unroll
+            for (int kk = 0; kk < ZC; ++kk) {
+                if (k0 + kk >= a.nz) break;
+                // clamp rows (the reference's texture clamps; no row range test)
+                const float rr = fminf(fmaxf(fmaf((float)kk, drr, rr0), 0.0f), rmax + 0.5f);
+                int ir;
+                float fr;
+                split_pos(rr, ir, fr);
+                const int r0 = min(max(ir - 1, 0), a.n_rows - 1), r1 = min(ir, a.n_rows - 1);
+                const float *ra = pv + (size_t)r0 * a.C, *rc = pv + (size_t)r1 * a.C;
+                const float va0 = __ldg(ra + i0), va1 = __ldg(ra + i1);
+                const float vc0 = __ldg(rc + i0), vc1 = __ldg(rc + i1);
+                const float lo = fmaf(f, va1 - va0, va0), hi = fmaf(f, vc1 - vc0, vc0);
+                acc[kk] = fmaf(fmaf(fr, hi - lo, lo), wgt, acc[kk]);
+            }
+        }
+    }
+    if (b < batch && ix < a.nx && iy < a.ny) {
+        float *vb = vol + (size_t)b * a.nz * a.ny * a.nx;
+#pragma unroll
+        for (int kk = 0; kk < ZC; ++kk)
+            if (k0 + kk < a.nz) vb[((size_t)(k0 + kk) * a.ny + iy) * a.nx + ix] = acc[kk];
+    }
+}
+
+// ---- CB_EA transpose ---------------------------------------------------------
+// Block = one view and RB detector rows of one volume; the block's rows of
+// the view accumulate in shared memory.  Threads sweep the FOV pixels; for
+// each they compute column, weight and row slope once and visit only the z
+// slices whose row coordinate reaches the block's rows.
+constexpr int kRB = 16;
+
+template <int DEG>
+__global__ void __launch_bounds__(kThreads)
+    cone_bp_transpose_kernel(const float *__restrict__ vol, float *__restrict__ proj,
+                             const float2 *__restrict__ view_cs, ConeArgs a, int batch) {
+    extern __shared__ float rows_acc[];  // [kRB][C]
+    const int rblocks = (a.n_rows + kRB - 1) / kRB;
+    const int v = blockIdx.x;
+    const int rb = blockIdx.y % rblocks, b = blockIdx.y / rblocks;
+    const int R0 = rb * kRB;
+    const int nr = min(kRB, a.n_rows - R0);
+    for (int k = threadIdx.x; k < kRB * a.C; k += kThreads) rows_acc[k] = 0.0f;
+    __syncthreads();
+    const float2 cs = __ldg(view_cs + v);
+    const float *vb = vol + (size_t)b * a.nz * a.ny * a.nx;
+    const float rmax = (float)a.n_rows;
+    const size_t plane = (size_t)a.nx * a.ny;
+    for (int p = threadIdx.x; p < a.nx * a.ny; p += kThreads) {
+        const int iy = p / a.nx, ix = p - iy * a.nx;
+        const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
+        const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
+        if (!(xd * xd + yd * yd <= a.fov_r2)) continue;
+        const float px = (float)xd, py = (float)yd;
+        const float U = fmaf(px, cs.x, fmaf(py, cs.y, a.R));
+        const float t = fmaf(py, cs.x, -px * cs.y);
+        const float rU = __fdividef(1.0f, U);
+        const float y = fmaf(cone_atan<DEG>(t * rU, a), a.inv_dcol, a.pos_off);
+        if (!(y > 0.5f && y < a.fC + 0.5f)) continue;
+        int ic;
+        float f;
+        split_pos(y, ic, f);
+        const int i0 = max(ic - 1, 0), i1 = min(ic, a.C - 1);
+        const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
+        const float slope = a.row_scale * rU;
+        const float rr_first = fmaf(a.zmin + 0.5f * a.dz, slope, a.row_off);  // slice 0
+        const float drr = a.dz * slope;
+        // slices whose row coordinate (clamped) touches rows [R0-1, R0+nr]:
+        // rr in (R0 - 0.5, R0 + nr + 0.5], widened by one slice each way
+        int klo = 0, khi = a.nz;
+        if (drr > 0.0f) {
+            const float lo = floorf((R0 - 1.0f - rr_first) / drr);
+            const float hi = ceilf((R0 + nr + 1.0f - rr_first) / drr) + 1.0f;
+            klo = (int)fminf(fmaxf(lo, 0.0f), (float)a.nz);
+            khi = (int)fminf(fmaxf(hi, 0.0f), (float)a.nz);
+            if (R0 == 0) klo = 0;
+            if (R0 + nr >= a.n_rows) khi = a.nz;
+        }
+        for (int k = klo; k < khi; ++k) {
+            const float val = __ldg(vb + (size_t)k * plane + p) * wgt;
+            if (val == 0.0f) continue;
+            const float rr = fminf(fmaxf(fmaf((float)k, drr, rr_first), 0.0f), rmax + 0.5f);
+            int ir;
+            float fr;
+            split_pos(rr, ir, fr);
+            const int r0 = min(max(ir - 1, 0), a.n_rows - 1) - R0;
+            const int r1 = min(ir, a.n_rows - 1) - R0;
+            if ((unsigned)r0 < (unsigned)nr) {
+                atomicAdd(&rows_acc[r0 * a.C + i0], val * (1.0f - fr) * (1.0f - f));
+                atomicAdd(&rows_acc[r0 * a.C + i1], val * (1.0f - fr) * f);
+            }
+            if ((unsigned)r1 < (unsigned)nr) {
+                atomicAdd(&rows_acc[r1 * a.C + i0], val * fr * (1.0f - f));
+                atomicAdd(&rows_acc[r1 * a.C + i1], val * fr * f);
+            }
+        }
+    }
+    __syncthreads();
+    float *pv = proj + ((size_t)b * a.V + v) * a.n_rows * a.C;
+    for (int k = threadIdx.x; k < nr * a.C; k += kThreads) pv[(size_t)R0 * a.C + k] = rows_acc[k];
+}
+
+// ---- cone-beam forward projection -----------------------------------------------
+// Warp = 32 consecutive channels of one view, as in the fan-beam projector:
+// the warp walks its rays' in-plane cells row-synchronously (transposed
+// volume when most rays run along x) and, per lane, handles RB detector rows
+// at once.  Detector row r sits at height h_r = det_bottom + (r+1/2) drow on
+// the cylinder of radius D about the source; at in-plane distance s the ray
+// is at height z = h_r s / D, so its z cell coordinate is linear in the
+// sample index.  Inside an in-plane cell the bilinear weights are quadratic
+// and the z fraction linear in the sample index, so each (cell, row) sum is
+// exact in closed form from sum j^m, m <= 3 (split where the z cell changes).
+// Weight: 0.125*dx*sqrt(1 + (h_r/D)^2), the 3-D length of one in-plane step.
+struct ConeFpArgs {
+    int V, C, nx, ny, nz, n_rows, wpv;
+    float w;        // 0.125*dx
+    float D, det_bottom, drow, dz, zmin;
+    int max_iter;
+};
+
+template <int RB>
+__global__ void __launch_bounds__(kThreads)
+    cone_fp_kernel(const float *__restrict__ vol, const float *__restrict__ vol_t,
+                   float *__restrict__ proj, const float4 *__restrict__ ray,
+                   const int *__restrict__ nsamp, const float2 *__restrict__ chan_s,
+                   ConeFpArgs a, int batch) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+    if (gw >= a.V * a.wpv) return;
+    const int rgroups = (a.n_rows + RB - 1) / RB;
+    const int b = blockIdx.y / rgroups;
+    const int r0 = (blockIdx.y - b * rgroups) * RB;
+    const int v = gw / a.wpv;
+    const int c = (gw - v * a.wpv) * 32 + lane;
+    const bool has_c = c < a.C;
+    const int r = v * a.C + (has_c ? c : a.C - 1);
+    const int n = has_c ? __ldg(nsamp + r) : 0;
+    const bool valid = n > 0;
+    const float4 q = valid ? __ldg(ray + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned vm = __ballot_sync(FULL, valid);
+    const unsigned xm = __ballot_sync(FULL, valid && fabsf(q.z) > fabsf(q.w));
+    const bool along_x = 2 * __popc(xm) > __popc(vm);
+    const RaySeg seg = along_x ? RaySeg{q.y - 0.5f, q.x - 0.5f, q.w, q.z}
+                               : RaySeg{q.x - 0.5f, q.y - 0.5f, q.z, q.w};
+    const int W = along_x ? a.ny : a.nx, H = along_x ? a.nx : a.ny;
+    const size_t plane = (size_t)a.nx * a.ny;
+    const float *vb = (along_x ? vol_t : vol) + (size_t)min(b, batch - 1) * a.nz * plane;
+    // z cell coordinate of sample k for row rr: w0[rr] + dw[rr] * k
+    // in-plane distance from the source of sample k: s0 - k * chord / n (mm)
+    const float2 sd = has_c ? __ldg(chan_s + c) : make_float2(0.f, 0.f);
+    const float ds = valid ? -sd.y / (float)n : 0.0f;
+    float w0[RB], dw[RB], acc[RB];
+#pragma unroll
+    for (int rr = 0; rr < RB; ++rr) {
+        const float h = a.det_bottom + a.drow * ((float)(r0 + rr) + 0.5f);
+        w0[rr] = (h * sd.x / a.D - a.zmin) / a.dz - 0.5f;
+        dw[rr] = h * ds / (a.D * a.dz);
+        acc[rr] = 0.0f;
+    }
+    // adds the closed-form sums of cell (cu, cv) for samples k .. k+cnt-1
+    auto cell = [&](int cu, int cv, float cnt, float fa, float fb, float k) {
+        // bilinear weights as quadratics in j: (1-fu)(1-fv), fu(1-fv), (1-fu)fv, fu fv
+        const float Au = 1.0f - fa, Av = 1.0f - fb;
+        const float q00[3] = {Au * Av, -(Au * seg.sv + Av * seg.su), seg.su * seg.sv};
+        const float q10[3] = {fa * Av, seg.su * Av - fa * seg.sv, -seg.su * seg.sv};
+        const float q01[3] = {Au * fb, Au * seg.sv - seg.su * fb, -seg.su * seg.sv};
+        const float q11[3] = {fa * fb, fa * seg.sv + fb * seg.su, seg.su * seg.sv};
+        const int i0 = min(max(cu, 0), W - 1), i1 = min(max(cu + 1, 0), W - 1);
+        const int j0 = min(max(cv, 0), H - 1) * W, j1 = min(max(cv + 1, 0), H - 1) * W;
+#pragma unroll
+        for (int rr = 0; rr < RB; ++rr) {
+            if (r0 + rr >= a.n_rows) break;
+            // z cells inside this cell's samples: split where floor(w) changes
+            float kk = k;
+            const float kend = k + cnt;
+            for (int t = 0; t < 16 && kk < kend; ++t) {  // every piece has >= 1 sample
+                const float wk = fmaf(dw[rr], kk, w0[rr]);
+                const float kz = floorf(wk);
+                // next z boundary in sample units
+                float kb = kend;
+                if (dw[rr] > 0.0f) kb = fminf(kend, ceilf((kz + 1.0f - w0[rr]) / dw[rr]));
+                else if (dw[rr] < 0.0f) kb = fminf(kend, ceilf((kz - w0[rr]) / dw[rr]));
+                if (!(kb > kk)) kb = kk + 1.0f;  // always progress
+                const float n_ = kb - kk;
+                const float j0f = kk - k;  // offset of this piece inside the cell
+                // sums over j = j0f .. j0f + n_ - 1
+                const float e = j0f + n_ - 1.0f;
+                const float S0 = n_;
+                const float S1 = 0.5f * (j0f + e) * n_;
+                // sum j^2 and j^3 over [j0f, e] from prefix formulas
+                const float P2e = e * (e + 1.0f) * (2.0f * e + 1.0f) * (1.0f / 6.0f);
+                const float P2s = (j0f - 1.0f) * j0f * (2.0f * j0f - 1.0f) * (1.0f / 6.0f);
+                const float P3e = 0.25f * e * e * (e + 1.0f) * (e + 1.0f);
+                const float P3s = 0.25f * (j0f - 1.0f) * (j0f - 1.0f) * j0f * j0f;
+                const float S2 = P2e - P2s, S3 = P3e - P3s;
+                // z fraction as a linear function of j: cz + dz_ j
+                const float cz = fmaf(dw[rr], k, w0[rr]) - kz;
+                const float dzj = dw[rr];
+                const int z0 = min(max((int)kz, 0), a.nz - 1), z1 = min(max((int)kz + 1, 0), a.nz - 1);
+                const float *p0 = vb + (size_t)z0 * plane, *p1 = vb + (size_t)z1 * plane;
+                const float t00[2] = {__ldg(p0 + j0 + i0), __ldg(p1 + j0 + i0)};
+                const float t10[2] = {__ldg(p0 + j0 + i1), __ldg(p1 + j0 + i1)};
+                const float t01[2] = {__ldg(p0 + j1 + i0), __ldg(p1 + j1 + i0)};
+                const float t11[2] = {__ldg(p0 + j1 + i1), __ldg(p1 + j1 + i1)};
+                auto sum2 = [&](const float *qq, const float *tt) {
+                    const float sq = qq[0] * S0 + qq[1] * S1 + qq[2] * S2;      // sum Q
+                    const float sqz = qq[0] * cz * S0 + (qq[0] * dzj + qq[1] * cz) * S1 +
+                                      (qq[1] * dzj + qq[2] * cz) * S2 + qq[2] * dzj * S3;  // sum Q fz
+                    return fmaf(sq - sqz, tt[0], sqz * tt[1]);
+                };
+                acc[rr] += sum2(q00, t00) + sum2(q10, t10) + sum2(q01, t01) + sum2(q11, t11);
+                kk = kb;
+            }
+        }
+    };
+    const unsigned pm = __ballot_sync(FULL, valid && seg.sv > 0.0f);
+    const int dir = 2 * __popc(pm) >= __popc(vm) ? 1 : -1;
+    const bool synced = valid && (dir > 0 ? seg.sv > 0.0f : seg.sv < 0.0f);
+    const float nf = (float)n;
+    const int jf = (int)floorf(seg.v0);
+    const int jl = (int)floorf(fmaf(seg.sv, nf - 1.0f, seg.v0));
+    int J0, J1;
+    if (dir > 0) {
+        J0 = __reduce_min_sync(FULL, synced ? jf : INT_MAX) - 1;
+        J1 = __reduce_max_sync(FULL, synced ? jl : INT_MIN) + 1;
+    } else {
+        J0 = __reduce_max_sync(FULL, synced ? jf : INT_MIN) + 1;
+        J1 = __reduce_min_sync(FULL, synced ? jl : INT_MAX) - 1;
+    }
+    if (__any_sync(FULL, synced)) {
+        const float INF = __int_as_float(0x7f800000);
+        const float iu = seg.su != 0.0f ? 1.0f / seg.su : 0.0f;
+        const float iv = synced ? 1.0f / seg.sv : 0.0f;
+        const float du = seg.su >= 0.0f ? 1.0f : -1.0f;
+        const int rows = (J1 - J0) * dir + 1;
+        for (int it = 0; it < rows; ++it) {
+            const int j = J0 + it * dir;
+            if (!synced) continue;
+            const float tA = ((float)j - seg.v0) * iv, tB = ((float)(j + 1) - seg.v0) * iv;
+            const float ka = fmaxf(0.0f, ceilf(fminf(tA, tB)));
+            const float kb = fminf(nf, ceilf(fmaxf(tA, tB)));
+            if (!(ka < kb)) continue;
+            float cu = floorf(fmaf(seg.su, ka, seg.u0));
+            float bu = seg.su >= 0.0f ? cu + 1.0f : cu;
+            float k = ka;
+            for (int t = 0; t < 8 && k < kb; ++t) {
+                const float tu = seg.su != 0.0f ? (bu - seg.u0) * iu : INF;
+                const float ke = fminf(kb, ceilf(tu));
+                const float cnt = ke - k;
+                if (cnt > 0.0f) {
+                    cell((int)cu, j, cnt, fmaf(seg.su, k, seg.u0) - cu,
+                         fmaf(seg.sv, k, seg.v0) - (float)j, k);
+                    k = ke;
+                }
+                cu += du;
+                bu += du;
+            }
+        }
+    }
+    if (valid && !synced) {
+        walk_cells(seg, 0.0f, nf, a.max_iter, [&](int cu, int cv, float cnt, float fa, float fb) {
+            // the walk gives the fractions at the cell's first sample; recover k
+            // from the u (or v) position: k = (cu + fa - u0) / su
+            const float kf = fabsf(seg.su) >= fabsf(seg.sv) ? rintf((cu + fa - seg.u0) / seg.su)
+                                                             : rintf((cv + fb - seg.v0) / seg.sv);
+            cell(cu, cv, cnt, fa, fb, kf);
+        });
+    }
+    if (has_c && b < batch) {
+        float *pv = proj + ((size_t)b * a.V + v) * a.n_rows * a.C;
+#pragma unroll
+        for (int rr = 0; rr < RB; ++rr) {
+            if (r0 + rr >= a.n_rows) break;
+            const float h = a.det_bottom + a.drow * ((float)(r0 + rr) + 0.5f);
+            pv[(size_t)(r0 + rr) * a.C + c] = acc[rr] * a.w * sqrtf(1.0f + (h / a.D) * (h / a.D));
+        }
+    }
+}
+
+// in [nz][ny][nx] planes -> out [nz][nx][ny]
+__global__ void __launch_bounds__(256)
+    transpose_planes_kernel(const float *__restrict__ in, float *__restrict__ out, int nx, int ny) {
+    __shared__ float t[32][33];
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const size_t plane = (size_t)nx * ny;
+    const float *src = in + blockIdx.z * plane;
+    float *dst = out + blockIdx.z * plane;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = x0 + threadIdx.x, y = y0 + j;
+        if (x < nx && y < ny) t[j][threadIdx.x] = src[(size_t)y * nx + x];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int y = y0 + threadIdx.x, x = x0 + j;
+        if (x < nx && y < ny) dst[(size_t)x * ny + y] = t[threadIdx.x][j];
+    }
+}
+
+ConeArgs make_cone_args(const ct_plan *p) {
+    ConeArgs a;
+    a.V = p->g.n_views;
+    a.C = p->g.n_cols;
+    a.nx = p->g.nx;
+    a.ny = p->g.ny;
+    a.nz = p->nz;
+    a.n_rows = p->n_rows;
+    a.xmin = p->g.xmin;
+    a.ymin = p->g.ymin;
+    a.dx = p->g.dx;
+    a.dy = p->g.dy;
+    a.dz = p->g.dz;
+    a.zmin = -0.5f * p->g.dz * (float)p->nz;
+    a.R = p->g.sid;
+    a.D = p->g.sdd;
+    const double inv = 1.0 / (double)p->g.dcol;
+    a.inv_dcol = (float)inv;
+    a.pos_off = (float)((double)p->g.shift - (double)p->g.left * inv + 0.5);
+    a.fC = (float)a.C;
+    a.row_scale = (float)((double)p->g.sdd / (double)p->g.drow);
+    a.row_off = (float)(-(double)p->g.det_bottom / (double)p->g.drow + 0.5);
+    a.fov_r2 = (double)p->g.rfov * (double)p->g.rfov;
+    for (int k = 0; k < 9; ++k) a.coef[k] = p->atan_coef[k];
+    a.atan_deg = p->atan_deg;
+    return a;
+}
+
+}  // namespace
+
+int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream) {
+    const ConeArgs a = make_cone_args(p);
+    constexpr int ZC = 16;
+    const int zgroups = (a.nz + ZC - 1) / ZC;
+    const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
+    for (int b0 = 0; b0 < batch; b0 += 4096) {
+        const int nb = batch - b0 < 4096 ? batch - b0 : 4096;
+        dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, zgroups * nb);
+        const float *pp = proj + (size_t)b0 * a.V * a.n_rows * a.C;
+        float *vp = vol + (size_t)b0 * a.nz * a.ny * a.nx;
+        cudaStream_t s = (cudaStream_t)stream;
+        if (a.atan_deg == 4)
+            cone_bp_kernel<ZC, 4><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, a, nb);
+        else if (a.atan_deg == 8)
+            cone_bp_kernel<ZC, 8><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, a, nb);
+        else
+            cone_bp_kernel<ZC, 0><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, a, nb);
+        ct_count_launch();
+    }
+    return (int)cudaGetLastError();
+}
+
+int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream) {
+    const ConeArgs a = make_cone_args(p);
+    const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
+    const size_t smem = sizeof(float) * kRB * a.C;
+    auto kern = a.atan_deg == 4   ? cone_bp_transpose_kernel<4>
+                : a.atan_deg == 8 ? cone_bp_transpose_kernel<8>
+                                  : cone_bp_transpose_kernel<0>;
+    cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    const int rblocks = (a.n_rows + kRB - 1) / kRB;
+    const int per = 65535 / rblocks;
+    for (int b0 = 0; b0 < batch; b0 += per) {
+        const int nb = batch - b0 < per ? batch - b0 : per;
+        kern<<<dim3(a.V, rblocks * nb), kThreads, smem, (cudaStream_t)stream>>>(
+            vol + (size_t)b0 * a.nz * a.ny * a.nx, proj + (size_t)b0 * a.V * a.n_rows * a.C, vcs,
+            a, nb);
+        ct_count_launch();
+    }
+    return (int)cudaGetLastError();
+}
+
+size_t cone_fp_work_bytes(const ct_plan *p, int batch) {
+    return sizeof(float) * (size_t)batch * p->nz * p->g.nx * p->g.ny;
+}
+
+int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work,
+            void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nx = p->g.nx, ny = p->g.ny, nz = p->nz;
+    float *vol_t = static_cast<float *>(work);
+    for (int b0 = 0; b0 < batch; ++b0) {
+        transpose_planes_kernel<<<dim3((nx + 31) / 32, (ny + 31) / 32, nz), dim3(32, 8), 0, s>>>(
+            vol + (size_t)b0 * nz * nx * ny, vol_t + (size_t)b0 * nz * nx * ny, nx, ny);
+        ct_count_launch();
+    }
+    ConeFpArgs a;
+    a.V = p->g.n_views;
+    a.C = p->g.n_cols;
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.n_rows = p->n_rows;
+    a.wpv = (a.C + 31) / 32;
+    a.w = p->fp_weight;
+    a.D = p->g.sdd;
+    a.det_bottom = p->g.det_bottom;
+    a.drow = p->g.drow;
+    a.dz = p->g.dz;
+    a.zmin = -0.5f * p->g.dz * (float)nz;
+    a.max_iter = 2 * (nx > ny ? nx : ny) + 8;
+    constexpr int RB = 8;
+    const int rgroups = (a.n_rows + RB - 1) / RB;
+    const int blocks = (a.V * a.wpv + kThreads / 32 - 1) / (kThreads / 32);
+    const int per = 65535 / rgroups;
+    for (int b0 = 0; b0 < batch; b0 += per) {
+        const int nb = batch - b0 < per ? batch - b0 : per;
+        cone_fp_kernel<RB><<<dim3(blocks, rgroups * nb), kThreads, 0, s>>>(
+            vol + (size_t)b0 * nz * nx * ny, vol_t + (size_t)b0 * nz * nx * ny,
+            proj + (size_t)b0 * a.V * a.n_rows * a.C, reinterpret_cast<const float4 *>(p->d_ray),
+            p->d_nsamp, reinterpret_cast<const float2 *>(p->d_chan_s), a, nb);
+        ct_count_launch();
+    }
+    return (int)cudaGetLastError();
+}
+
+}  // namespace ctk

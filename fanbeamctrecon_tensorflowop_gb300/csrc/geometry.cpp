@@ -250,3 +250,24 @@ int ct_fit_atan(double zmax, float coef[9]) {
     }
     return 0;
 }
+
+// In-plane geometry of the cone-beam projector's rays, per channel i (the
+// same for every view): with gamma = left + (i+1/2) dcol, the ray's distance
+// from the isocentre is d = R sin(gamma), its FOV chord 2 sqrt(rfov^2 - d^2),
+// and its first sample (the far chord end) lies R cos(gamma) + sqrt(rfov^2 -
+// d^2) from the source; both in mm, evaluated in pixel units as the ray table.
+void ct_build_channel_table(const ct_fan_geom *g, ct_host_tables *t) {
+    const int C = g->n_cols;
+    t->chan_s.assign(2 * (size_t)C, 0.0f);
+    const double dx = g->dx;
+    const double src_px = (double)g->sid / dx, fov_px = (double)g->rfov / dx;
+    for (int i = 0; i < C; ++i) {
+        const double gam = (double)g->left + (i + 0.5) * (double)g->dcol;
+        const double dist = src_px * std::sin(gam);
+        const double h = fov_px * fov_px - dist * dist;
+        if (!(h > 0.0)) continue;
+        const double x1 = -std::sqrt(h);
+        t->chan_s[2 * i + 0] = static_cast<float>(dx * (src_px * std::cos(gam) - x1));
+        t->chan_s[2 * i + 1] = static_cast<float>(dx * 2.0 * std::sqrt(h));
+    }
+}

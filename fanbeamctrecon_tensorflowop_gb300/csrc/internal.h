@@ -25,6 +25,9 @@ struct ct_host_tables {
     std::vector<float> ray;          // [4*V*C]
     std::vector<int32_t> nsamp;      // [V*C]
     std::vector<float> taps;         // [2C-1] ramp filter taps, index n + C - 1
+    // Per channel: in-plane distance (mm) from the source to the ray's first
+    // sample, and the FOV chord length (mm) (cone-beam projector heights).
+    std::vector<float> chan_s;       // [2*C]
     int32_t max_nsamp = 0;
     double total_samples = 0;        // sum of nsamp over all rays
 };
@@ -35,6 +38,7 @@ ct_status ct_validate_geom(const ct_fan_geom *g);
 void ct_build_view_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
 void ct_build_ray_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
 void ct_build_filter_taps(const ct_fan_geom *g, int window, ct_host_tables *t);
+void ct_build_channel_table(const ct_fan_geom *g, ct_host_tables *t);
 // Largest |t/U| = tan(gamma) over the FOV disc: rfov / sqrt(R^2 - rfov^2).
 double ct_max_tan_gamma(const ct_fan_geom *g);
 // Fits atan(z) = z * sum_k coef[k] (z^2)^k on |z| <= zmax (interpolation at
@@ -49,6 +53,7 @@ struct ct_plan {
     int filter_algo;                 // resolved ct_filter_algo (never AUTO)
     float fp_weight;                 // 0.125*dx (FP/transform.cu:144)
     float fov_r2;                    // rfov^2 (BP/transform.cu:116)
+    int n_rows, nz;                  // cone plans; 1 and 1 for fan plans
     int atan_deg;                    // 4 or 8: polynomial atan on the FOV; 0: atanf
     float atan_coef[9];
     double total_samples;
@@ -59,6 +64,7 @@ struct ct_plan {
     float *d_ray;                    // [4VC]
     int32_t *d_nsamp;                // [VC]
     float *d_taps;                   // [2C-1]
+    float *d_chan_s;                 // [2C]
 };
 
 // Kernel launchers (defined in the .cu files).  Each returns the launch error.
@@ -74,6 +80,10 @@ int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch,
                      void *stream);
 int ramp_filter(const ct_plan *p, const float *in, float *out, int rows, void *stream);
 size_t ramp_direct_smem(int C);
+int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream);
+int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream);
+int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work, void *stream);
+size_t cone_fp_work_bytes(const ct_plan *p, int batch);
 int plain_fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *stream);
 int plain_fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
 int plain_bp_fan(const ct_plan *p, const float *sino, float *img, int batch, void *stream);

@@ -28,6 +28,9 @@ def _ptr(t: torch.Tensor | None) -> int | None:
 class FanPlan:
     """A fan-beam geometry bound to one CUDA device."""
 
+    n_rows = 1
+    nz = 1
+
     def __init__(self, param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK,
                  filter_algo: int = _lib.FILTER_AUTO):
         self._lib = _lib.load()
@@ -45,12 +48,14 @@ class FanPlan:
         opts.filter_algo = int(filter_algo)
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            st = self._lib.ct_plan_create(
-                ctypes.byref(self.geom),
-                self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
-                int(self.angles.shape[0]), ctypes.byref(opts), ctypes.byref(handle))
+            st = self._create(opts, handle)
         _lib.check(st, "ct_plan_create")
         self._h = handle
+
+    def _create(self, opts, handle) -> int:
+        return self._lib.ct_plan_create(
+            ctypes.byref(self.geom), self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+            int(self.angles.shape[0]), ctypes.byref(opts), ctypes.byref(handle))
 
     # -- lifetime ---------------------------------------------------------------
     def close(self) -> None:
@@ -185,6 +190,80 @@ class FanPlan:
     def plain_bp(self, sino: torch.Tensor) -> torch.Tensor:
         y = self._check_in(sino, self.sino_shape, "sinogram")
         return self._run("ct_plain_bp_fan", None, y, self.image_shape, False)
+
+
+class ConePlan(FanPlan):
+    """A cone-beam geometry: the fan geometry of ``param16`` (parameter[13..15]
+    = detector bottom, row height, slice thickness) with ``n_rows`` detector
+    rows and ``nz`` slices.  Volumes are float32 [B, nz, ny, nx], projections
+    float32 [B, n_views, n_rows, n_cols]."""
+
+    def __init__(self, param16, angles, n_rows: int, nz: int, device=None,
+                 window: int = _lib.WINDOW_RAMLAK):
+        self.n_rows = int(n_rows)
+        self.nz = int(nz)
+        super().__init__(param16, angles, device=device, window=window)
+
+    def _create(self, opts, handle) -> int:
+        return self._lib.ct_plan_create_cone(
+            ctypes.byref(self.geom), self.n_rows, self.nz,
+            self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+            int(self.angles.shape[0]), ctypes.byref(opts), ctypes.byref(handle))
+
+    @property
+    def volume_shape(self) -> tuple[int, int, int]:
+        return (self.nz, self.geom.ny, self.geom.nx)
+
+    @property
+    def proj_shape(self) -> tuple[int, int, int]:
+        return (self.geom.n_views, self.n_rows, self.geom.n_cols)
+
+    def _check4(self, t: torch.Tensor, tail, what: str) -> torch.Tensor:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{what} must be a torch.Tensor")
+        if t.device != self.device or t.dtype != torch.float32:
+            raise ValueError(f"{what} must be float32 on {self.device}")
+        if t.dim() == 3:
+            t = t.unsqueeze(0)
+        if t.dim() != 4 or tuple(t.shape[1:]) != tuple(tail):
+            raise ValueError(f"{what} must be [B, {', '.join(map(str, tail))}], got "
+                             f"{tuple(t.shape)}")
+        return t.contiguous()
+
+    def _run4(self, name, op, x, out_tail, out=None):
+        B = x.shape[0]
+        if out is None:
+            out = torch.empty((B, *out_tail), dtype=torch.float32, device=self.device)
+        fn = getattr(self._lib, name)
+        with torch.cuda.device(self.device):
+            if op is None:
+                st = fn(self._h, _ptr(x), _ptr(out), B, self._stream())
+            else:
+                work, nbytes = self._work(op, B)
+                st = fn(self._h, _ptr(x), _ptr(out), B, _ptr(work), nbytes, self._stream())
+        _lib.check(st, name)
+        return out
+
+    def fp_cone(self, vol: torch.Tensor, out=None) -> torch.Tensor:
+        """Cone-beam forward projection."""
+        x = self._check4(vol, self.volume_shape, "volume")
+        return self._run4("ct_fp_cone", _lib.OP_FP_CONE, x, self.proj_shape, out)
+
+    def cone_bp(self, proj: torch.Tensor, out=None) -> torch.Tensor:
+        """The reference's CB_EA backprojection (unfiltered)."""
+        y = self._check4(proj, self.proj_shape, "projections")
+        return self._run4("ct_cone_bp", None, y, self.volume_shape, out)
+
+    def fdk(self, proj: torch.Tensor, out=None) -> torch.Tensor:
+        """FDK: ramp filter per (view, row), then the CB_EA backprojection."""
+        y = self._check4(proj, self.proj_shape, "projections")
+        return self._run4("ct_fdk_cone", _lib.OP_FDK_CONE, y, self.volume_shape, out)
+
+    def fdk_adjoint(self, vol: torch.Tensor, out=None) -> torch.Tensor:
+        """Exact transpose of ``fdk``."""
+        x = self._check4(vol, self.volume_shape, "volume")
+        return self._run4("ct_fdk_cone_adjoint", _lib.OP_FDK_CONE_ADJOINT, x, self.proj_shape,
+                          out)
 
 
 def get_plan(param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK) -> FanPlan:

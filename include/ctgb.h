@@ -114,7 +114,10 @@ typedef enum ct_op {
     CT_OP_FBP = 3,
     CT_OP_FBP_ADJOINT = 4,
     CT_OP_FDK_BP = 5,
-    CT_OP_BP_ADJOINT = 6
+    CT_OP_BP_ADJOINT = 6,
+    CT_OP_FP_CONE = 7,
+    CT_OP_FDK_CONE = 8,
+    CT_OP_FDK_CONE_ADJOINT = 9
 } ct_op;
 
 typedef struct ct_plan ct_plan;
@@ -223,6 +226,46 @@ ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_s
  * FDK/GPURecon_GPU.cu:178-179) and the output is zeroed first. */
 ct_status ct_fdk_bp(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
                     void *d_work, size_t work_bytes, ct_stream stream);
+
+/* ---- cone beam ------------------------------------------------------------- */
+/* Volumes are float32 [batch][nz][ny][nx], voxel centres z = zmin + dz(k+1/2)
+ * with zmin = -dz*nz/2 (FDK/FBP.cc:86); projections are float32
+ * [batch][n_views][n_rows][n_cols] (the view layout of the reference's FDK
+ * filter, FDK/GPURecon_GPU.cu:211).  Detector row r is at height
+ * det_bottom + (r+1/2)*drow; the source orbits at z = 0.  geom->det_bottom,
+ * drow and dz are parameter[13..15] of the FDK op (FDK/FBP.cc:82-84). */
+
+/* A plan for nz slices and n_rows detector rows (the reference's FDK op fixes
+ * both to 1, FDK/FBP.cc:85,98; ct_plan_create makes such a plan).  Requires
+ * drow > 0, dz > 0 and sdd > sid. */
+ct_status ct_plan_create_cone(const ct_fan_geom *geom, int n_rows, int nz, const float *angles,
+                              int n_angles, const ct_plan_opts *opts, ct_plan **out);
+
+/* The reference's CB_EA backprojection (FDK/GPURecon_GPU.cu:15-50) over all
+ * views, unfiltered: per voxel in the FOV disc and view, the bilinear
+ * (col, row) sample of the view with col as in ct_bp_fan and
+ * row = (z*D/U - det_bottom)/drow (clamped rows), times 1/(U^2+t^2). */
+ct_status ct_cone_bp(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,
+                     ct_stream stream);
+
+/* FDK: ramp filter of every (view, row), then ct_cone_bp.  Replaces
+ * BP_One_Rot_3D_GPU (FDK/GPURecon_GPU.cu:163-268) for nz, n_rows >= 1. */
+ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,
+                      void *d_work, size_t work_bytes, ct_stream stream);
+
+/* Exact adjoint of ct_fdk_cone (CB_EA transpose, then the symmetric filter):
+ * d_vol -> d_proj.  No counterpart in the reference. */
+ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_proj, int batch,
+                              void *d_work, size_t work_bytes, ct_stream stream);
+
+/* Cone-beam forward projection, d_vol -> d_proj.  No counterpart in the
+ * reference (only its unused 3-D textures, FDK/GPURecon_GPU.cu:10,12, remain).
+ * The ray from the source to detector cell (view, row r, channel i) is
+ * sampled at the fan-beam projector's in-plane positions; at in-plane
+ * distance s from the source its height is h_r*s/D.  Samples are trilinear
+ * and clamp-to-edge; the sum is weighted by 0.125*dx*sqrt(1 + (h_r/D)^2). */
+ct_status ct_fp_cone(const ct_plan *plan, const float *d_vol, float *d_proj, int batch,
+                     void *d_work, size_t work_bytes, ct_stream stream);
 
 /* ---- filtered backprojection that allocates nothing ----------------------- */
 

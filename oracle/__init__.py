@@ -87,6 +87,12 @@ def _l():
         lib.orc_fbp_fan.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
         lib.orc_fbp_fan_adjoint.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
         lib.orc_fdk_bp.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
+        ci = ctypes.c_int
+        lib.orc_cone_bp.argtypes = [g, ci, ci, fp_, dp, dp, ci]
+        lib.orc_cone_bp_transpose.argtypes = [g, ci, ci, fp_, dp, dp, ci]
+        lib.orc_fdk_cone.argtypes = [g, ci, ci, fp_, ci, dp, dp, ci]
+        lib.orc_fdk_cone_adjoint.argtypes = [g, ci, ci, fp_, ci, dp, dp, ci]
+        lib.orc_cone_fp.argtypes = [g, ci, ci, fp_, dp, dp, ci]
         _lib = lib
     return _lib
 
@@ -220,4 +226,64 @@ def fdk_bp(g, angles, sino, window: int = RAMLAK) -> np.ndarray:
     out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
     _l().orc_fdk_bp(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(y), _dptr(out),
                     y.shape[0])
+    return out
+
+
+# ---- cone beam: volume [B][nz][ny][nx], projections [B][V][n_rows][C] ----------
+
+def _batch_vol(g, nz, vol):
+    x = _f64(vol)
+    if x.ndim == 3:
+        x = x[None]
+    if x.shape[1:] != (nz, g.ny, g.nx):
+        raise ValueError(f"volume must be [B,{nz},{g.ny},{g.nx}], got {x.shape}")
+    return x
+
+
+def _batch_proj(g, n_rows, proj):
+    y = _f64(proj)
+    if y.ndim == 3:
+        y = y[None]
+    if y.shape[1:] != (g.n_views, n_rows, g.n_cols):
+        raise ValueError(f"projections must be [B,{g.n_views},{n_rows},{g.n_cols}], got {y.shape}")
+    return y
+
+
+def cone_fp(g, n_rows, nz, angles, vol) -> np.ndarray:
+    x = _batch_vol(g, nz, vol)
+    out = np.zeros((x.shape[0], g.n_views, n_rows, g.n_cols), np.float64)
+    _l().orc_cone_fp(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(x),
+                     _dptr(out), x.shape[0])
+    return out
+
+
+def cone_bp(g, n_rows, nz, angles, proj) -> np.ndarray:
+    y = _batch_proj(g, n_rows, proj)
+    out = np.zeros((y.shape[0], nz, g.ny, g.nx), np.float64)
+    _l().orc_cone_bp(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(y),
+                     _dptr(out), y.shape[0])
+    return out
+
+
+def cone_bp_transpose(g, n_rows, nz, angles, vol) -> np.ndarray:
+    x = _batch_vol(g, nz, vol)
+    out = np.zeros((x.shape[0], g.n_views, n_rows, g.n_cols), np.float64)
+    _l().orc_cone_bp_transpose(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(x),
+                               _dptr(out), x.shape[0])
+    return out
+
+
+def fdk_cone(g, n_rows, nz, angles, proj, window: int = RAMLAK) -> np.ndarray:
+    y = _batch_proj(g, n_rows, proj)
+    out = np.zeros((y.shape[0], nz, g.ny, g.nx), np.float64)
+    _l().orc_fdk_cone(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), window, _dptr(y),
+                      _dptr(out), y.shape[0])
+    return out
+
+
+def fdk_cone_adjoint(g, n_rows, nz, angles, vol, window: int = RAMLAK) -> np.ndarray:
+    x = _batch_vol(g, nz, vol)
+    out = np.zeros((x.shape[0], g.n_views, n_rows, g.n_cols), np.float64)
+    _l().orc_fdk_cone_adjoint(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), window,
+                              _dptr(x), _dptr(out), x.shape[0])
     return out

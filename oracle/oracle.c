@@ -451,3 +451,197 @@ void orc_fdk_bp(const orc_geom *g, const float *angles, int window, const double
     }
     free(filt);
 }
+
+/* ---- cone beam ------------------------------------------------------------
+ * Volume [B][nz][ny][nx]; projections [B][V][n_rows][C] (the reference's view
+ * layout, FDK/GPURecon_GPU.cu:211: view * nCols * nRows + row * nCols).
+ * Voxel centres: x = xmin + dx(i+1/2), y likewise, z = zmin + dz(k+1/2) with
+ * zmin = -dz*nz/2 (FDK/FBP.cc:86); the source orbits at z = 0
+ * (FDK/GPURecon_GPU.cu:226). */
+
+/* CB_EA backprojection, FDK/GPURecon_GPU.cu:25-49, for any nz and n_rows:
+ * per voxel in the FOV disc and view, col = (atan(t/U) - left)/dcol + shift
+ * (0 < col < C), row = (z * D / U - det_bottom) / drow, bilinear clamped
+ * sample of the [n_rows][C] view at (col, row), weight 1/(U^2+t^2). */
+static void cone_bp_impl(const orc_geom *g, int n_rows, int nz, const float *angles,
+                         const double *proj, double *vol, int batch, int transpose) {
+    const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
+    const double r2 = (double)g->rfov * (double)g->rfov;
+    const float zmin = -0.5f * g->dz * (float)nz;
+    const size_t pview = (size_t)n_rows * C, pvol = (size_t)nz * ny * nx;
+    if (transpose) memset((void *)proj, 0, sizeof(double) * batch * V * pview);
+    for (int b = 0; b < batch; ++b) {
+        const double *pb = proj + (size_t)b * V * pview;
+        double *vb = vol + (size_t)b * pvol;
+        if (!transpose) {
+#pragma omp parallel for schedule(dynamic, 2)
+            for (int j = 0; j < ny; ++j) {
+                const double y = (double)g->ymin + (double)g->dy * (j + 0.5);
+                for (int i = 0; i < nx; ++i) {
+                    const double x = (double)g->xmin + (double)g->dx * (i + 0.5);
+                    for (int k = 0; k < nz; ++k) vb[((size_t)k * ny + j) * nx + i] = 0.0;
+                    if (!(x * x + y * y <= r2)) continue;
+                    for (int v = 0; v < V; ++v) {
+                        const double beta = angles[v];
+                        const double c = -cos(beta), s = -sin(beta);
+                        int i0, i1;
+                        double f, U, t;
+                        if (!bp_col(g, x, y, c, s, &i0, &i1, &f, &U, &t)) continue;
+                        const double wgt = 1.0 / (U * U + t * t);
+                        const double *pv = pb + (size_t)v * pview;
+                        for (int k = 0; k < nz; ++k) {
+                            const double zk = (double)zmin + (double)g->dz * (k + 0.5);
+                            const double row =
+                                (zk * (double)g->sdd / U - (double)g->det_bottom) / (double)g->drow;
+                            const double rb = row - 0.5, rf = floor(rb);
+                            const double fr = frac_w(rb - rf);
+                            const int q = (int)rf;
+                            const int ra = q < 0 ? 0 : (q > n_rows - 1 ? n_rows - 1 : q);
+                            const int rc = q + 1 < 0 ? 0 : (q + 1 > n_rows - 1 ? n_rows - 1 : q + 1);
+                            const double *va = pv + (size_t)ra * C, *vc = pv + (size_t)rc * C;
+                            const double lo = (1.0 - f) * va[i0] + f * va[i1];
+                            const double hi = (1.0 - f) * vc[i0] + f * vc[i1];
+                            vb[((size_t)k * ny + j) * nx + i] += ((1.0 - fr) * lo + fr * hi) * wgt;
+                        }
+                    }
+                }
+            }
+        } else {
+            double *pw = (double *)(proj + (size_t)b * V * pview);
+#pragma omp parallel for schedule(dynamic, 2)
+            for (int v = 0; v < V; ++v) {
+                const double beta = angles[v];
+                const double c = -cos(beta), s = -sin(beta);
+                double *pv = pw + (size_t)v * pview;
+                for (int j = 0; j < ny; ++j) {
+                    const double y = (double)g->ymin + (double)g->dy * (j + 0.5);
+                    for (int i = 0; i < nx; ++i) {
+                        const double x = (double)g->xmin + (double)g->dx * (i + 0.5);
+                        int i0, i1;
+                        double f, U, t;
+                        if (!(x * x + y * y <= r2)) continue;
+                        if (!bp_col(g, x, y, c, s, &i0, &i1, &f, &U, &t)) continue;
+                        const double wgt = 1.0 / (U * U + t * t);
+                        for (int k = 0; k < nz; ++k) {
+                            const double val = vb[((size_t)k * ny + j) * nx + i] * wgt;
+                            const double zk = (double)zmin + (double)g->dz * (k + 0.5);
+                            const double row =
+                                (zk * (double)g->sdd / U - (double)g->det_bottom) / (double)g->drow;
+                            const double rb = row - 0.5, rf = floor(rb);
+                            const double fr = frac_w(rb - rf);
+                            const int q = (int)rf;
+                            const int ra = q < 0 ? 0 : (q > n_rows - 1 ? n_rows - 1 : q);
+                            const int rc = q + 1 < 0 ? 0 : (q + 1 > n_rows - 1 ? n_rows - 1 : q + 1);
+                            if (val == 0.0) continue;
+                            pv[(size_t)ra * C + i0] += val * (1.0 - fr) * (1.0 - f);
+                            pv[(size_t)ra * C + i1] += val * (1.0 - fr) * f;
+                            pv[(size_t)rc * C + i0] += val * fr * (1.0 - f);
+                            pv[(size_t)rc * C + i1] += val * fr * f;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+void orc_cone_bp(const orc_geom *g, int n_rows, int nz, const float *angles, const double *proj,
+                 double *vol, int batch) {
+    cone_bp_impl(g, n_rows, nz, angles, proj, vol, batch, 0);
+}
+
+void orc_cone_bp_transpose(const orc_geom *g, int n_rows, int nz, const float *angles,
+                           const double *vol, double *proj, int batch) {
+    cone_bp_impl(g, n_rows, nz, angles, proj, (double *)vol, batch, 1);
+}
+
+/* FDK of the reference (BP_One_Rot_3D_GPU, FDK/GPURecon_GPU.cu:163-268) with
+ * nz slices and n_rows detector rows: ramp filter every (view, row), then the
+ * CB_EA backprojection.  orc_fdk_bp is its nz = n_rows = 1 case. */
+void orc_fdk_cone(const orc_geom *g, int n_rows, int nz, const float *angles, int window,
+                  const double *proj, double *vol, int batch) {
+    const size_t n = (size_t)batch * g->n_views * n_rows * g->n_cols;
+    double *filt = (double *)malloc(sizeof(double) * (n ? n : 1));
+    orc_ramp_filter(g, window, proj, filt, (long)batch * g->n_views * n_rows);
+    orc_cone_bp(g, n_rows, nz, angles, filt, vol, batch);
+    free(filt);
+}
+
+/* Transpose of orc_fdk_cone: CB_EA transpose, then the symmetric filter. */
+void orc_fdk_cone_adjoint(const orc_geom *g, int n_rows, int nz, const float *angles, int window,
+                          const double *vol, double *proj, int batch) {
+    const size_t n = (size_t)batch * g->n_views * n_rows * g->n_cols;
+    double *tmp = (double *)malloc(sizeof(double) * (n ? n : 1));
+    orc_cone_bp_transpose(g, n_rows, nz, angles, vol, tmp, batch);
+    orc_ramp_filter(g, window, tmp, proj, (long)batch * g->n_views * n_rows);
+    free(tmp);
+}
+
+/* Cone-beam forward projection (no reference counterpart: the reference
+ * removed its cone projector and kept only unused 3-D textures,
+ * FDK/GPURecon_GPU.cu:10,12).  Detector cell (view v, row r, channel i) is
+ * the point at height h_r = det_bottom + (r+1/2) drow on the cylinder of
+ * radius D about the source, at fan angle left + (i+1/2) dcol.  The ray from
+ * the source to it is sampled at the in-plane positions of the fan-beam
+ * projector (start + k*step, k < n, orc_ray_table); at in-plane distance s
+ * from the source the ray's height is z = h_r * s / D.  Each sample is a
+ * trilinear, clamp-to-edge volume sample (texel centres at +1/2 in x, y, z),
+ * and the sum is weighted by 0.125*dx*sqrt(1 + (h_r/D)^2), the 3-D length of
+ * one in-plane step. */
+void orc_cone_fp(const orc_geom *g, int n_rows, int nz, const float *angles, const double *vol,
+                 double *proj, int batch) {
+    const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
+    const size_t R = (size_t)V * C;
+    double *ray = (double *)malloc(sizeof(double) * 4 * R);
+    int32_t *ns = (int32_t *)malloc(sizeof(int32_t) * R);
+    const double dx = g->dx, D = g->sdd;
+    const double src = (double)g->sid / dx, fov = (double)g->rfov / dx;
+    const float zmin = -0.5f * g->dz * (float)nz;
+    const size_t pvol = (size_t)nz * ny * nx;
+    orc_ray_table(g, angles, ray, ns);
+    for (int b = 0; b < batch; ++b) {
+        const double *vb = vol + (size_t)b * pvol;
+        double *pb = proj + (size_t)b * V * n_rows * C;
+#pragma omp parallel for schedule(dynamic, 16)
+        for (long rr = 0; rr < (long)R; ++rr) {
+            const int v = (int)(rr / C), i = (int)(rr % C);
+            const double *q = ray + 4 * rr;
+            const int n = ns[rr];
+            /* in-plane distance (mm) from the source of sample k: s0 + k*ds */
+            const double gam = (double)g->left + (i + 0.5) * (double)g->dcol;
+            const double dist = src * sin(gam);
+            const double h = fov * fov - dist * dist;
+            double s0 = 0.0, ds = 0.0;
+            if (n > 0) {
+                const double x1 = -sqrt(h);
+                const double L = 2.0 * sqrt(h);
+                s0 = dx * (src * cos(gam) - x1);
+                ds = -dx * L / n;
+            }
+            for (int r = 0; r < n_rows; ++r) {
+                const double hr = (double)g->det_bottom + (r + 0.5) * (double)g->drow;
+                double acc = 0.0;
+                for (int k = 0; k < n; ++k) {
+                    const tap4 t = bilinear_taps(nx, ny, q[0] + k * q[2], q[1] + k * q[3]);
+                    const double z = hr * (s0 + k * ds) / D;
+                    const double wz = (z - (double)zmin) / (double)g->dz - 0.5;
+                    const double fz0 = floor(wz);
+                    const double az = frac_w(wz - fz0);
+                    const int kz = (int)fz0;
+                    const int k0 = kz < 0 ? 0 : (kz > nz - 1 ? nz - 1 : kz);
+                    const int k1 = kz + 1 < 0 ? 0 : (kz + 1 > nz - 1 ? nz - 1 : kz + 1);
+                    const double *p0 = vb + (size_t)k0 * ny * nx, *p1 = vb + (size_t)k1 * ny * nx;
+                    const double a0 = t.w00 * p0[t.j0 * nx + t.i0] + t.w10 * p0[t.j0 * nx + t.i1] +
+                                      t.w01 * p0[t.j1 * nx + t.i0] + t.w11 * p0[t.j1 * nx + t.i1];
+                    const double a1 = t.w00 * p1[t.j0 * nx + t.i0] + t.w10 * p1[t.j0 * nx + t.i1] +
+                                      t.w01 * p1[t.j1 * nx + t.i0] + t.w11 * p1[t.j1 * nx + t.i1];
+                    acc += (1.0 - az) * a0 + az * a1;
+                }
+                pb[((size_t)v * n_rows + r) * C + i] =
+                    acc * ORC_STEP * dx * sqrt(1.0 + (hr / D) * (hr / D));
+            }
+        }
+    }
+    free(ray);
+    free(ns);
+}

@@ -56,3 +56,19 @@ def fdk_driver(nview=96, ncol=888, nimg=64):
     p[15] = 2.5
     a = (np.arange(nview) * (2.0 * math.pi / nview)).astype(np.float32)
     return p, a
+
+
+def cone_small(n=32, views=48, cols=64, n_rows=12, nz=10, pixel=5.6, dz=3.0, drow=6.0):
+    """A small cone geometry whose detector covers the volume in z:
+    |z| <= nz*dz/2 magnifies by at most D/(R - rFOV) onto rows of height drow."""
+    p = fan_param16(sdd=SDD, sid=SID, n_views=views, n_cols=cols, n=n, pixel_mm=pixel,
+                    dcol_rad=4.0 * DCOL, det_bottom=-n_rows * drow / 2.0, drow=drow, dz=dz)
+    return p, angle(views, 0.0), n_rows, nz
+
+
+def config4(views=984, cols=888, n_rows=64, nz=64, n=512):
+    """Clinical cone geometry: 984 views, 888 x 64 detector (1 mm rows at the
+    detector, bottom -32 mm), 512^2 x 64 voxels of 0.7 x 0.7 x 0.625 mm."""
+    p = fan_param16(sdd=SDD, sid=SID, n_views=views, n_cols=cols, n=n, pixel_mm=0.7,
+                    dcol_rad=DCOL, det_bottom=-n_rows / 2.0, drow=1.0, dz=0.625)
+    return p, angle(views, 0.0), n_rows, nz

@@ -1,0 +1,122 @@
+"""Cone-beam operators on the GPU against the FP64 oracle, through the C ABI.
+Tolerance as for the fan-beam operators: relative L2 <= 1e-4, adjoint
+dot-product mismatch <= 1e-5."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from fanbeamctrecon_tensorflowop_gb300 import _lib, phantom
+from fanbeamctrecon_tensorflowop_gb300.ops import ConePlan, FanPlan
+import geometries as G
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+DOT_TOL = 1e-5
+
+
+def _t(a, dev):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+
+
+def _np(t):
+    torch.cuda.synchronize()
+    return t.detach().cpu().numpy().astype(np.float64)
+
+
+def _vol(g, nz, batch, seed=0):
+    out = []
+    for b in range(batch):
+        sl = phantom.ellipse_phantom(g.nx, float(g.dx), seed=seed + b, ny=g.ny)
+        w = 1.0 + 0.3 * np.sin(np.linspace(0, 3, nz))[:, None, None]
+        out.append(sl[None] * w)
+    return np.stack(out).astype(np.float32)
+
+
+CASES = {
+    "small": lambda: G.cone_small(),
+    "odd": lambda: G.cone_small(n=27, views=31, cols=57, n_rows=7, nz=9, pixel=6.6),
+}
+
+
+@pytest.fixture(scope="module", params=list(CASES))
+def cone(request, cuda, orc):
+    p, a, nr, nz = CASES[request.param]()
+    plan = ConePlan(p, a, nr, nz, device=cuda)
+    plan_sl = ConePlan(p, a, nr, nz, device=cuda, window=_lib.WINDOW_SHEPP_LOGAN)
+    return p, a, nr, nz, plan, plan_sl, orc.decode(p)
+
+
+def test_cone_fp(cone, cuda, orc):
+    p, a, nr, nz, plan, _, g = cone
+    x = _vol(g, nz, 2)
+    got = _np(plan.fp_cone(_t(x, cuda)))
+    ref = orc.cone_fp(g, nr, nz, a, x)
+    assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
+
+
+def test_cone_bp_and_fdk(cone, cuda, orc):
+    p, a, nr, nz, plan, plan_sl, g = cone
+    y = orc.cone_fp(g, nr, nz, a, _vol(g, nz, 2, seed=3))
+    got = _np(plan.cone_bp(_t(y, cuda)))
+    ref = orc.cone_bp(g, nr, nz, a, y)
+    assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
+    for pl, w in ((plan, orc.RAMLAK), (plan_sl, orc.SHEPP_LOGAN)):
+        got = _np(pl.fdk(_t(y, cuda)))
+        ref = orc.fdk_cone(g, nr, nz, a, y, w)
+        assert rel_l2(got, ref) <= TOL, (w, rel_l2(got, ref))
+
+
+def test_fdk_adjoint(cone, cuda, orc):
+    p, a, nr, nz, plan, _, g = cone
+    x = _vol(g, nz, 2, seed=5)
+    got = _np(plan.fdk_adjoint(_t(x, cuda)))
+    ref = orc.fdk_cone_adjoint(g, nr, nz, a, x)
+    assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
+    rng = np.random.default_rng(1)
+    xx = rng.standard_normal((2, nz, g.ny, g.nx)).astype(np.float32)
+    yy = rng.standard_normal((2, g.n_views, nr, g.n_cols)).astype(np.float32)
+    ax = _np(plan.fdk_adjoint(_t(xx, cuda)))
+    aty = _np(plan.fdk(_t(yy, cuda)))
+    m = abs(float(np.vdot(ax, yy)) - float(np.vdot(xx, aty))) / (
+        np.linalg.norm(ax) * np.linalg.norm(yy))
+    assert m <= DOT_TOL, m
+
+
+def test_fdk_cone_single_row_matches_fan_fdk_op(cuda):
+    p, a = G.fdk_driver(nview=60, nimg=48)
+    cone = ConePlan(p, a, 1, 1, device=cuda)
+    fan = FanPlan(p, a, device=cuda)
+    y = torch.rand((2, 60, 888), device=cuda)
+    v3 = cone.fdk(y.reshape(2, 60, 1, 888))
+    v2 = fan.fdk_bp(y)
+    assert rel_l2(_np(v3[:, 0]), _np(v2)) < 1e-6
+
+
+def test_fdk_cone_autograd(cuda):
+    from fanbeamctrecon_tensorflowop_gb300.autograd import fdk_cone
+    p, a, nr, nz = G.cone_small(n=24, views=20, cols=48, n_rows=6, nz=5)
+    plan = ConePlan(p, a, nr, nz, device=cuda)
+    y = torch.rand((1, *plan.proj_shape), device=cuda, requires_grad=True)
+    target = torch.rand((1, *plan.volume_shape), device=cuda)
+    loss = 0.5 * ((fdk_cone(y, plan) - target) ** 2).sum()
+    loss.backward()
+    with torch.no_grad():
+        expect = plan.fdk_adjoint(plan.fdk(y) - target)
+    assert rel_l2(_np(y.grad), _np(expect)) < 1e-6
+
+
+def test_cone_errors(cuda):
+    p, a, nr, nz = G.cone_small()
+    with pytest.raises(_lib.CtError):
+        ConePlan(p, a, 0, nz, device=cuda)
+    bad = p.copy()
+    bad[14] = 0.0  # drow
+    with pytest.raises(_lib.CtError):
+        ConePlan(bad, a, nr, nz, device=cuda)
+    plan = ConePlan(p, a, nr, nz, device=cuda)
+    with pytest.raises(ValueError):
+        plan.fdk(torch.zeros((1, 3, nr, 64), device=cuda))

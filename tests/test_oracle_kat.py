@@ -180,3 +180,45 @@ def test_texture_emulation_bounds_reference_deviation(orc):
         orc.set_texture_emulation(False)
     d = rel_l2(tex, exact)
     assert 1e-6 < d < 1e-2
+
+
+# ---- cone beam ---------------------------------------------------------------
+
+def test_fdk_cone_one_row_one_slice_is_the_fdk_op(orc):
+    """With nz = n_rows = 1 (FDK/FBP.cc:85,98) the cone FDK is the 2-D op."""
+    p, a = G.fdk_driver(nview=40, nimg=32)
+    g = orc.decode(p)
+    y = np.random.default_rng(2).uniform(0, 1, (1, g.n_views, 1, g.n_cols))
+    np.testing.assert_allclose(orc.fdk_cone(g, 1, 1, a, y)[:, 0], orc.fdk_bp(g, a, y[:, :, 0]),
+                               rtol=1e-13, atol=1e-16)
+
+
+def test_cone_adjoint_identities(orc):
+    p, a, nr, nz = G.cone_small(n=20, views=12, cols=40, n_rows=6, nz=5)
+    g = orc.decode(p)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((1, nz, g.ny, g.nx))
+    y = rng.standard_normal((1, g.n_views, nr, g.n_cols))
+    for ax, aty in ((orc.cone_bp_transpose(g, nr, nz, a, x), orc.cone_bp(g, nr, nz, a, y)),
+                    (orc.fdk_cone_adjoint(g, nr, nz, a, x), orc.fdk_cone(g, nr, nz, a, y))):
+        lhs, rhs = float(np.vdot(ax, y)), float(np.vdot(x, aty))
+        assert abs(lhs - rhs) <= 1e-12 * np.linalg.norm(ax) * np.linalg.norm(y)
+
+
+def test_cone_fp_known_answers(orc):
+    """A constant volume projects to 0.125*dx*n*sqrt(1+(h_r/D)^2) (trilinear of
+    a constant, clamp-to-edge in z); a z-invariant volume projects to the fan
+    FP of its slice times the same stretch factor."""
+    p, a, nr, nz = G.cone_small(n=24, views=10, cols=48, n_rows=8, nz=6)
+    g = orc.decode(p)
+    _, ns = orc.ray_table(g, a)
+    h = g.det_bottom + (np.arange(nr) + 0.5) * g.drow
+    stretch = np.sqrt(1 + (h / g.sdd) ** 2)
+    ones = orc.cone_fp(g, nr, nz, a, np.ones((nz, g.ny, g.nx)))[0]
+    np.testing.assert_allclose(ones, 0.125 * g.dx * ns[:, None, :] * stretch[None, :, None],
+                               rtol=1e-12, atol=0)
+    sl = phantom.ellipse_phantom(24, float(g.dx), seed=4).astype(np.float64)
+    cyl = orc.cone_fp(g, nr, nz, a, np.repeat(sl[None], nz, axis=0))[0]
+    fan = orc.fp_fan(g, a, sl)[0]
+    np.testing.assert_allclose(cyl, fan[:, None, :] * stretch[None, :, None], rtol=1e-10,
+                               atol=1e-12)
