@@ -203,6 +203,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cone", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -345,6 +346,41 @@ def main() -> None:
         barrier()
         plain_ms = 1e3 * max_over_ranks(time.perf_counter() - t0) / n_plain
 
+    # ---- cone beam, batch of 4 volumes (512^2 x 64 @0.7x0.7x0.625 mm, 984 views,
+    #      888 x 64 detector): cone FP -> FDK -> FDK adjoint --------------------------------
+    cone = None
+    if not args.no_cone:
+        from fanbeamctrecon_tensorflowop_gb300.geometry import fan_param16 as _f16
+        from fanbeamctrecon_tensorflowop_gb300.ops import ConePlan
+        cp = _f16(sdd=SDD, sid=SID, n_views=VIEWS, n_cols=COLS, n=N_PIX, pixel_mm=PIXEL_MM,
+                  dcol_rad=DCOL, det_bottom=-32.0, drow=1.0, dz=0.625)
+        cplan = ConePlan(cp, a, 64, 64, device=dev)
+        CB = 4
+        cvol = torch.rand((CB, 64, N_PIX, N_PIX), device=dev, generator=gen)
+        cproj = cplan.fp_cone(cvol)
+        crec = cplan.fdk(cproj)
+        cgrad = cplan.fdk_adjoint(crec)
+
+        def cone_time(fn):
+            fn()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            barrier()
+            return max_over_ranks(e0.elapsed_time(e1)) / CB
+
+        t_fp = cone_time(lambda: cplan.fp_cone(cvol, out=cproj))
+        t_fdk = cone_time(lambda: cplan.fdk(cproj, out=crec))
+        t_adj = cone_time(lambda: cplan.fdk_adjoint(crec, out=cgrad))
+        cone = {"workload": "cone beam, 4 volumes 512x512x64 @0.7x0.7x0.625 mm, 984 views, "
+                            "888 x 64 detector (1 mm rows), FP -> FDK -> FDK adjoint",
+                "fp_cone_ms_per_volume": t_fp, "fdk_ms_per_volume": t_fdk,
+                "fdk_adjoint_ms_per_volume": t_adj,
+                "fdk_gvoxel_views_per_s": 512 * 512 * 64 * VIEWS / t_fdk / 1e6}
+        del cvol, cproj, crec, cgrad
+
     # ---- e2e through the reference-named entry point with host buffers ---------------
     host_imgs = [imgs[k].cpu().numpy() for k in range(2)]
     vs, ps = [BATCH, N_PIX, N_PIX], [BATCH, VIEWS, COLS]
@@ -391,6 +427,7 @@ def main() -> None:
                 "plain_batch32_fp_adjoint_ms": plain_ms,
                 "speedup_vs_plain": (plain_ms / fa_ms) if plain_ms else None,
                 "fp_samples_per_slice": plan.total_samples,
+                "cone": cone,
             },
         }
         print(json.dumps(line))
