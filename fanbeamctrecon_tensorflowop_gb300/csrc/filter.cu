@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(kThreads)
 size_t ramp_direct_smem(int C) { return sizeof(float) * ((2 * C - 1 + 3) / 4 * 4 + kRows * C); }
 
 int ramp_filter(const ct_plan *p, const float *in, float *out, int rows, void *stream) {
+    if (p->filter_algo == CT_FILTER_TOEPLITZ_TC) return ramp_filter_tc(p, in, out, rows, stream);
     const int C = p->g.n_cols;
     const size_t smem = ramp_direct_smem(C);
     const bool odd_only = p->opts.filter_window == CT_WINDOW_RAMLAK;

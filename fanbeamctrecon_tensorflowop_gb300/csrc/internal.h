@@ -65,6 +65,8 @@ struct ct_plan {
     int32_t *d_nsamp;                // [VC]
     float *d_taps;                   // [2C-1]
     float *d_chan_s;                 // [2C]
+    float *d_tc_hi, *d_tc_lo;        // tensor-core filter: TF32 split of the Toeplitz taps
+    int *d_err;                      // raised by kernels whose bounded waits gave up
 };
 
 // Kernel launchers (defined in the .cu files).  Each returns the launch error.
@@ -80,6 +82,10 @@ int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch,
                      void *stream);
 int ramp_filter(const ct_plan *p, const float *in, float *out, int rows, void *stream);
 size_t ramp_direct_smem(int C);
+int tc_padded(int C);
+bool ramp_tc_supported(int C);
+void build_tc_taps(const float *taps, int C, std::vector<float> &hi, std::vector<float> &lo);
+int ramp_filter_tc(const ct_plan *p, const float *in, float *out, int rows, void *stream);
 int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream);
 int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream);
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work, void *stream);

@@ -96,8 +96,11 @@ typedef enum ct_filter_window {
 /* How the row filter executes on the device. */
 typedef enum ct_filter_algo {
     CT_FILTER_AUTO = 0,      /* the library picks (measured fastest accurate path) */
-    CT_FILTER_DIRECT = 1,    /* FP32 direct convolution, odd taps only */
-    CT_FILTER_TOEPLITZ_TC = 2 /* Toeplitz GEMM on tcgen05 tensor cores, BF16x3 split */
+    CT_FILTER_DIRECT = 1,    /* FP32 direct convolution (Ram-Lak: odd taps only) */
+    /* Toeplitz GEMM on the tcgen05 tensor cores: TF32 three-term split
+     * (x_hi*h_hi + x_hi*h_lo + x_lo*h_hi), FP32 accumulation in tensor
+     * memory; needs n_cols % 4 == 0 and n_cols <= 4032. */
+    CT_FILTER_TOEPLITZ_TC = 2
 } ct_filter_algo;
 
 typedef struct ct_plan_opts {
@@ -159,6 +162,10 @@ ct_status ct_fp_ray_table(const ct_fan_geom *geom, const float *angles, int n_an
 ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_angles,
                          const ct_plan_opts *opts, ct_plan **out);
 ct_status ct_plan_destroy(ct_plan *plan);
+/* Waits for the device and reports CT_ERR_TIMEOUT (and clears the flag) if
+ * a kernel of this plan hit the iteration limit of one of its bounded waits
+ * since the last check (only the tensor-core filter waits on barriers). */
+ct_status ct_plan_check(const ct_plan *plan);
 /* The geometry a plan was built from. */
 ct_status ct_plan_geom(const ct_plan *plan, ct_fan_geom *out);
 
