@@ -57,6 +57,18 @@ class CtFanGeom(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class CtBatchItem(ctypes.Structure):
+    """Mirror of ct_batch_item."""
+
+    _fields_ = [("plan", ctypes.c_void_p), ("op", ctypes.c_int32), ("dtype", ctypes.c_int32),
+                ("d_in", ctypes.c_void_p), ("d_out", ctypes.c_void_p)]
+
+
+DTYPE_F32 = 0
+DTYPE_BF16 = 1
+BATCH_MAX_ITEMS = 64
+
+
 class CtPlanOpts(ctypes.Structure):
     _fields_ = [("filter_window", ctypes.c_int32), ("filter_algo", ctypes.c_int32),
                 ("reserved", ctypes.c_int32 * 6)]
@@ -95,6 +107,8 @@ SIGNATURES = {
     "ct_fdk_cone": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_fdk_cone_adjoint": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_fp_cone": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
+    "ct_batch_workspace_size": (_i, [_P(CtBatchItem), _i, _P(_sz)]),
+    "ct_batch_run": (_i, [_P(CtBatchItem), _i, _vp, _sz, _vp]),
     "ct_fbp_fan_static_scratch": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan_adjoint": (_i, [_vp, _vp, _vp, _i, _vp]),

@@ -480,6 +480,24 @@ ct_status ct_fp_cone(const ct_plan *plan, const float *d_vol, float *d_proj, int
     return launch_status(ctk::cone_fp(plan, d_vol, d_proj, batch, w.ptr, stream), "ct_fp_cone");
 }
 
+ct_status ct_batch_workspace_size(const ct_batch_item *items, int n, size_t *bytes) {
+    if (!bytes) return CT_ERR_NULL_POINTER;
+    return ctk::batch_workspace(items, n, bytes);
+}
+
+ct_status ct_batch_run(const ct_batch_item *items, int n, void *d_work, size_t work_bytes,
+                       ct_stream stream) {
+    size_t need = 0;
+    ct_status st = ctk::batch_workspace(items, n, &need);
+    if (st != CT_OK || n == 0) return st;
+    DeviceScope ds(items[0].plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, need, stream);
+    if (st != CT_OK) return st;
+    return launch_status(ctk::batch_run(items, n, w.ptr, stream), "ct_batch_run");
+}
+
 ct_status ct_plain_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,
                           ct_stream stream) {
     ct_status st = check_call(plan, d_img, d_sino, batch);

@@ -1,0 +1,407 @@
+// Uneven batches: one call runs FP, BP, FBP and FBP-adjoint work on up to
+// CT_BATCH_MAX_ITEMS slices whose geometries (image size, views, channels)
+// differ, with FP32 or BF16 storage and FP32 arithmetic throughout.
+//
+//   1. one launch builds the quad images of every FP item;
+//   2. one persistent FP launch: warps pull (item, view, 32-channel) units
+//      until all items' rays are projected (fp_warp, fp_body.cuh);
+//   3. per item: BF16 inputs are widened, FBP items are ramp-filtered with
+//      their plan's filter (the tensor-core Toeplitz GEMM where it applies),
+//      FBP-adjoint items run the weighted-BP transpose and the filter;
+//   4. one persistent BP launch: blocks pull (item, 32x32 tile) units of every
+//      BP / FBP item (bp_tile, bp_body.cuh);
+//   5. one launch narrows the FBP-adjoint results that are stored as BF16.
+// Item descriptors travel as __grid_constant__ kernel parameters, so a call
+// needs no host-to-device copy and can be captured in a CUDA graph.
+#include <cuda_bf16.h>
+
+#include <vector>
+
+#include "bp_body.cuh"
+#include "fp_body.cuh"
+
+namespace ctk {
+namespace {
+
+constexpr int kMax = CT_BATCH_MAX_ITEMS;
+
+struct QuadItem {
+    const void *img;
+    float4 *quads;
+    int nx, ny, bf16;
+    int blocks_x, blocks_y;  // of this item's 32 x 8 quad blocks
+    int unit0;               // first block index of this item
+};
+struct QuadBatch {
+    int n, total;
+    QuadItem it[kMax];
+};
+
+struct FpItem {
+    const float4 *quads;
+    void *out;
+    const float4 *ray;
+    const int *nsamp;
+    int V, C, wpv, nx, max_iter, out_bf16, unit0;
+    float w;
+};
+struct FpBatch {
+    int n, total;
+    FpItem it[kMax];
+};
+
+struct BpItem {
+    const float *sino;
+    void *img;
+    const float2 *view_cs;
+    BpArgs a;
+    int tiles_x, unit0, out_bf16, weighted, use_atanf;
+};
+struct BpBatch {
+    int n, total;
+    BpItem it[kMax];
+};
+
+struct ConvItem {
+    const void *src;
+    void *dst;
+    long long count;
+    int to_bf16;
+};
+struct ConvBatch {
+    int n;
+    ConvItem it[kMax];
+};
+
+template <typename Item>
+__device__ __forceinline__ int find_item(const Item *it, int n, int unit) {
+    int i = 0;
+    while (i + 1 < n && it[i + 1].unit0 <= unit) ++i;
+    return i;
+}
+
+__global__ void __launch_bounds__(256) quads_batch_kernel(const __grid_constant__ QuadBatch P) {
+    for (int u = blockIdx.x; u < P.total; u += gridDim.x) {
+        const QuadItem &it = P.it[find_item(P.it, P.n, u)];
+        const int local = u - it.unit0;
+        const int per_layout = it.blocks_x * it.blocks_y;
+        const int layout = local / per_layout, rem = local - layout * per_layout;
+        const int by = rem / it.blocks_x, bx = rem - by * it.blocks_x;
+        const int Q = it.nx + 1;
+        const int qi = bx * 32 + threadIdx.x, qj = by * 8 + threadIdx.y;
+        if (qi >= Q || qj >= Q) continue;
+        float4 *dst = it.quads + (size_t)layout * Q * Q + (size_t)qj * Q + qi;
+        if (it.bf16)
+            build_quad(static_cast<const __nv_bfloat16 *>(it.img), dst, it.nx, it.ny, layout, qi,
+                       qj);
+        else
+            build_quad(static_cast<const float *>(it.img), dst, it.nx, it.ny, layout, qi, qj);
+    }
+}
+
+__global__ void __launch_bounds__(256) fp_batch_kernel(const __grid_constant__ FpBatch P) {
+    const int step = gridDim.x * 8;
+    for (int gw = blockIdx.x * 8 + (threadIdx.x >> 5); gw < P.total; gw += step) {
+        const FpItem &it = P.it[find_item(P.it, P.n, gw)];  // warp-uniform
+        const int unit = gw - it.unit0;
+        if (it.out_bf16)
+            fp_warp<1, __nv_bfloat16>(it.quads, 0, static_cast<__nv_bfloat16 *>(it.out), 0,
+                                      it.ray, it.nsamp, it.V, it.C, it.wpv, it.nx, it.w, 1,
+                                      it.max_iter, unit);
+        else
+            fp_warp<1, float>(it.quads, 0, static_cast<float *>(it.out), 0, it.ray, it.nsamp,
+                              it.V, it.C, it.wpv, it.nx, it.w, 1, it.max_iter, unit);
+    }
+}
+
+template <bool W, int DEG>
+__device__ __forceinline__ void bp_item_tile(const BpItem &it, int tx, int ty) {
+    if (it.out_bf16)
+        bp_tile<W, 1, DEG, __nv_bfloat16>(it.sino, 0, static_cast<__nv_bfloat16 *>(it.img), 0,
+                                          it.view_cs, it.a, 1, tx, ty);
+    else
+        bp_tile<W, 1, DEG, float>(it.sino, 0, static_cast<float *>(it.img), 0, it.view_cs, it.a,
+                                  1, tx, ty);
+}
+
+__global__ void __launch_bounds__(256) bp_batch_kernel(const __grid_constant__ BpBatch P) {
+    for (int u = blockIdx.x; u < P.total; u += gridDim.x) {  // block-uniform
+        const BpItem &it = P.it[find_item(P.it, P.n, u)];
+        const int local = u - it.unit0;
+        const int ty = local / it.tiles_x, tx = local - ty * it.tiles_x;
+        if (it.use_atanf) {
+            if (it.weighted)
+                bp_item_tile<true, 0>(it, tx, ty);
+            else
+                bp_item_tile<false, 0>(it, tx, ty);
+        } else {
+            if (it.weighted)
+                bp_item_tile<true, 8>(it, tx, ty);
+            else
+                bp_item_tile<false, 8>(it, tx, ty);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) convert_batch_kernel(const __grid_constant__ ConvBatch P) {
+    const ConvItem &it = P.it[blockIdx.y];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < it.count;
+         k += stride) {
+        if (it.to_bf16)
+            static_cast<__nv_bfloat16 *>(it.dst)[k] =
+                __float2bfloat16(static_cast<const float *>(it.src)[k]);
+        else
+            static_cast<float *>(it.dst)[k] =
+                __bfloat162float(static_cast<const __nv_bfloat16 *>(it.src)[k]);
+    }
+}
+
+BpArgs bp_args(const ct_plan *p) {
+    BpArgs a;
+    a.V = p->g.n_views;
+    a.C = p->g.n_cols;
+    a.nx = p->g.nx;
+    a.ny = p->g.ny;
+    a.xmin = p->g.xmin;
+    a.ymin = p->g.ymin;
+    a.dx = p->g.dx;
+    a.dy = p->g.dy;
+    a.R = p->g.sid;
+    const double inv = 1.0 / (double)p->g.dcol;
+    a.inv_dcol = (float)inv;
+    a.pos_off = (float)((double)p->g.shift - (double)p->g.left * inv + 0.5);
+    a.fC = (float)a.C;
+    a.fov_r2 = (double)p->g.rfov * (double)p->g.rfov;
+    // degree-4 fits are the degree-8 polynomial with zero high coefficients
+    for (int k = 0; k < 9; ++k) a.coef[k] = p->atan_coef[k];
+    return a;
+}
+
+size_t align256(size_t n) { return (n + 255) / 256 * 256; }
+
+struct Layout {
+    // byte offsets into the workspace, per item (SIZE_MAX = unused)
+    std::vector<size_t> quads, in32, filt, out32;
+    size_t total = 0;
+};
+
+Layout plan_layout(const ct_batch_item *items, int n) {
+    Layout L;
+    L.quads.assign(n, SIZE_MAX);
+    L.in32.assign(n, SIZE_MAX);
+    L.filt.assign(n, SIZE_MAX);
+    L.out32.assign(n, SIZE_MAX);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += align256(bytes);
+        return o;
+    };
+    for (int i = 0; i < n; ++i) {
+        const ct_plan *p = items[i].plan;
+        const size_t img = sizeof(float) * (size_t)p->g.nx * p->g.ny;
+        const size_t sino = sizeof(float) * (size_t)p->g.n_views * p->g.n_cols;
+        const bool bf = items[i].dtype == CT_DTYPE_BF16;
+        switch (items[i].op) {
+            case CT_OP_FP:
+                L.quads[i] = take(sizeof(float4) * 2 * (size_t)(p->g.nx + 1) * (p->g.nx + 1));
+                break;
+            case CT_OP_BP:
+                if (bf) L.in32[i] = take(sino);
+                break;
+            case CT_OP_FBP:
+                if (bf) L.in32[i] = take(sino);
+                L.filt[i] = take(sino);
+                break;
+            case CT_OP_FBP_ADJOINT:
+                if (bf) L.in32[i] = take(img);
+                L.filt[i] = take(sino);
+                if (bf) L.out32[i] = take(sino);
+                break;
+            default:
+                break;
+        }
+    }
+    L.total = off;
+    return L;
+}
+
+ct_status check_items(const ct_batch_item *items, int n) {
+    if (n < 0 || n > kMax) return CT_ERR_INVALID_ARGUMENT;
+    if (n > 0 && !items) return CT_ERR_NULL_POINTER;
+    for (int i = 0; i < n; ++i) {
+        const ct_batch_item &it = items[i];
+        if (!it.plan || !it.d_in || !it.d_out) return CT_ERR_NULL_POINTER;
+        if (it.plan->n_rows != 1 || it.plan->nz != 1) return CT_ERR_INVALID_ARGUMENT;
+        if (it.dtype != CT_DTYPE_F32 && it.dtype != CT_DTYPE_BF16) return CT_ERR_INVALID_ARGUMENT;
+        if (it.op != CT_OP_FP && it.op != CT_OP_BP && it.op != CT_OP_FBP &&
+            it.op != CT_OP_FBP_ADJOINT)
+            return CT_ERR_INVALID_ARGUMENT;
+        if (it.d_in == it.d_out) return CT_ERR_INVALID_ARGUMENT;
+        if (it.plan->device != items[0].plan->device) return CT_ERR_INVALID_ARGUMENT;
+        if ((it.op == CT_OP_FBP || it.op == CT_OP_FBP_ADJOINT) &&
+            it.plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+            ramp_direct_smem(it.plan->g.n_cols) > 227 * 1024)
+            return CT_ERR_UNSUPPORTED;
+    }
+    return CT_OK;
+}
+
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace
+
+ct_status batch_workspace(const ct_batch_item *items, int n, size_t *bytes) {
+    ct_status st = check_items(items, n);
+    if (st != CT_OK) return st;
+    *bytes = plan_layout(items, n).total;
+    return CT_OK;
+}
+
+// Enqueues the whole batch on `stream`; returns a CUDA error code.
+int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const Layout L = plan_layout(items, n);
+    uint8_t *ws = static_cast<uint8_t *>(work);
+    auto at = [&](size_t off) { return static_cast<void *>(ws + off); };
+    const int sms = sm_count();
+    cudaError_t e;
+
+    // 1-2: forward projections
+    {
+        QuadBatch QB{};
+        FpBatch FB{};
+        for (int i = 0; i < n; ++i) {
+            if (items[i].op != CT_OP_FP) continue;
+            const ct_plan *p = items[i].plan;
+            const int Q = p->g.nx + 1;
+            QuadItem &q = QB.it[QB.n++];
+            q.img = items[i].d_in;
+            q.quads = static_cast<float4 *>(at(L.quads[i]));
+            q.nx = p->g.nx;
+            q.ny = p->g.ny;
+            q.bf16 = items[i].dtype == CT_DTYPE_BF16;
+            q.blocks_x = (Q + 31) / 32;
+            q.blocks_y = (Q + 7) / 8;
+            q.unit0 = QB.total;
+            QB.total += 2 * q.blocks_x * q.blocks_y;
+            FpItem &f = FB.it[FB.n++];
+            f.quads = q.quads;
+            f.out = items[i].d_out;
+            f.ray = reinterpret_cast<const float4 *>(p->d_ray);
+            f.nsamp = p->d_nsamp;
+            f.V = p->g.n_views;
+            f.C = p->g.n_cols;
+            f.wpv = (f.C + 31) / 32;
+            f.nx = p->g.nx;
+            f.max_iter = 2 * (p->g.nx > p->g.ny ? p->g.nx : p->g.ny) + 8;
+            f.out_bf16 = q.bf16;
+            f.w = p->fp_weight;
+            f.unit0 = FB.total;
+            FB.total += f.V * f.wpv;
+        }
+        if (QB.n > 0) {
+            quads_batch_kernel<<<QB.total < sms * 16 ? QB.total : sms * 16, dim3(32, 8), 0, s>>>(
+                QB);
+            fp_batch_kernel<<<(FB.total + 7) / 8 < sms * 3 ? (FB.total + 7) / 8 : sms * 3, 256, 0,
+                              s>>>(FB);
+            ct_count_launch(2);
+            if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
+        }
+    }
+    // 3: widen BF16 inputs of the BP / FBP / FBP-adjoint items
+    {
+        ConvBatch CB{};
+        int maxc = 0;
+        for (int i = 0; i < n; ++i) {
+            if (items[i].op == CT_OP_FP || items[i].dtype != CT_DTYPE_BF16) continue;
+            const ct_plan *p = items[i].plan;
+            const long long cnt = items[i].op == CT_OP_FBP_ADJOINT
+                                      ? (long long)p->g.nx * p->g.ny
+                                      : (long long)p->g.n_views * p->g.n_cols;
+            CB.it[CB.n++] = ConvItem{items[i].d_in, at(L.in32[i]), cnt, 0};
+            maxc = cnt > maxc ? (int)cnt : maxc;
+        }
+        if (CB.n > 0) {
+            const int bx = (maxc + 255) / 256 < 1024 ? (maxc + 255) / 256 : 1024;
+            convert_batch_kernel<<<dim3(bx, CB.n), 256, 0, s>>>(CB);
+            ct_count_launch();
+            if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
+        }
+    }
+    // filters (FBP) and transposes + filters (FBP adjoint), per item
+    for (int i = 0; i < n; ++i) {
+        const ct_plan *p = items[i].plan;
+        const bool bf = items[i].dtype == CT_DTYPE_BF16;
+        const float *in32 = bf ? static_cast<const float *>(at(L.in32[i]))
+                               : static_cast<const float *>(items[i].d_in);
+        if (items[i].op == CT_OP_FBP) {
+            if ((e = (cudaError_t)ramp_filter(p, in32, static_cast<float *>(at(L.filt[i])),
+                                              p->g.n_views, s)) != cudaSuccess)
+                return (int)e;
+        } else if (items[i].op == CT_OP_FBP_ADJOINT) {
+            float *t = static_cast<float *>(at(L.filt[i]));
+            if ((e = (cudaError_t)bp_fan_transpose(p, in32, t, 1, 1, s)) != cudaSuccess)
+                return (int)e;
+            float *dst = bf ? static_cast<float *>(at(L.out32[i]))
+                            : static_cast<float *>(items[i].d_out);
+            if ((e = (cudaError_t)ramp_filter(p, t, dst, p->g.n_views, s)) != cudaSuccess)
+                return (int)e;
+        }
+    }
+    // 4: backprojections of BP and FBP items
+    {
+        BpBatch BB{};
+        for (int i = 0; i < n; ++i) {
+            if (items[i].op != CT_OP_BP && items[i].op != CT_OP_FBP) continue;
+            const ct_plan *p = items[i].plan;
+            const bool bf = items[i].dtype == CT_DTYPE_BF16;
+            BpItem &b = BB.it[BB.n++];
+            if (items[i].op == CT_OP_FBP)
+                b.sino = static_cast<const float *>(at(L.filt[i]));
+            else
+                b.sino = bf ? static_cast<const float *>(at(L.in32[i]))
+                            : static_cast<const float *>(items[i].d_in);
+            b.img = items[i].d_out;
+            b.view_cs = reinterpret_cast<const float2 *>(p->d_view_cs);
+            b.a = bp_args(p);
+            b.tiles_x = (p->g.nx + kBpTile - 1) / kBpTile;
+            b.unit0 = BB.total;
+            b.out_bf16 = bf;
+            b.weighted = items[i].op == CT_OP_FBP;
+            b.use_atanf = p->atan_deg == 0;
+            BB.total += b.tiles_x * ((p->g.ny + kBpTile - 1) / kBpTile);
+        }
+        if (BB.n > 0) {
+            bp_batch_kernel<<<BB.total < sms * 4 ? BB.total : sms * 4, dim3(32, 8), 0, s>>>(BB);
+            ct_count_launch();
+            if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
+        }
+    }
+    // 5: narrow the BF16 FBP-adjoint results
+    {
+        ConvBatch CB{};
+        int maxc = 0;
+        for (int i = 0; i < n; ++i) {
+            if (items[i].op != CT_OP_FBP_ADJOINT || items[i].dtype != CT_DTYPE_BF16) continue;
+            const ct_plan *p = items[i].plan;
+            const long long cnt = (long long)p->g.n_views * p->g.n_cols;
+            CB.it[CB.n++] = ConvItem{at(L.out32[i]), items[i].d_out, cnt, 1};
+            maxc = cnt > maxc ? (int)cnt : maxc;
+        }
+        if (CB.n > 0) {
+            const int bx = (maxc + 255) / 256 < 1024 ? (maxc + 255) / 256 : 1024;
+            convert_batch_kernel<<<dim3(bx, CB.n), 256, 0, s>>>(CB);
+            ct_count_launch();
+        }
+    }
+    return (int)cudaGetLastError();
+}
+
+}  // namespace ctk

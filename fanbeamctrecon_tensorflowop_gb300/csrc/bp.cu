@@ -15,113 +15,22 @@
 // for up to four slices.  t/U uses the SFU reciprocal; atan(z) is a
 // polynomial in z^2 fitted per plan over the FOV's |z| range (to FP32 atanf
 // accuracy, 3e-8 absolute), with atanf kept for fans wider than 90 degrees.
-#include "common.cuh"
+#include "bp_body.cuh"
 
 namespace ctk {
 namespace {
 
-constexpr int kTile = 32;       // tile edge (pixels)
-constexpr int kRowsPerThr = 4;  // 32x8 threads cover 32x32 pixels
-
-struct BpArgs {
-    int V, C, nx, ny;
-    float xmin, ymin, dx, dy;
-    float R;
-    float inv_dcol;   // 1/dcol
-    float pos_off;    // shift - left/dcol + 1/2: y = atan*inv_dcol + pos_off = col + 1/2
-    float fC;         // n_cols
-    double fov_r2;
-    float coef[9];    // atan(z) = z * sum coef[k] z^(2k)
-};
-
-template <int DEG>
-__device__ __forceinline__ float fov_atan(float z, const float *c) {
-    if constexpr (DEG == 0) {
-        return atanf(z);
-    } else {
-        const float s = z * z;
-        float p = c[DEG];
-#pragma unroll
-        for (int k = DEG - 1; k >= 0; --k) p = fmaf(p, s, c[k]);
-        return z * p;
-    }
-}
-
-// y = col + 1/2 >= 0: i = trunc(y) = floor(col - 1/2) + 1 and f = frac(y),
-// without float-to-int conversion instructions (valid for 0 <= y < 2^22).
-__device__ __forceinline__ void split_pos(float y, int &i, float &f) {
-    const float m = __fadd_rz(y, 12582912.0f);
-    i = __float_as_int(m) - 0x4B400000;
-    f = y - (m - 12582912.0f);
-}
+constexpr int kTile = kBpTile;
+constexpr int kRowsPerThr = kBpRowsPerThr;
 
 template <bool WEIGHTED, int SB, int DEG>
 __global__ void __launch_bounds__(256)
     bp_fan_kernel(const float *__restrict__ sino, float *__restrict__ img,
                   const float2 *__restrict__ view_cs, BpArgs a, int batch) {
-    const int ix = blockIdx.x * kTile + threadIdx.x;
-    const int iy0 = blockIdx.y * kTile + threadIdx.y;
     const int b0 = blockIdx.z * SB;
-    float py[kRowsPerThr];
-    bool in[kRowsPerThr];
-    const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
-    const float px = (float)xd;
-    bool any = false;
-#pragma unroll
-    for (int k = 0; k < kRowsPerThr; ++k) {
-        const int iy = iy0 + 8 * k;
-        const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
-        py[k] = (float)yd;
-        in[k] = ix < a.nx && iy < a.ny && (xd * xd + yd * yd <= a.fov_r2);
-        any |= in[k];
-    }
-    float acc[SB][kRowsPerThr];
-#pragma unroll
-    for (int s = 0; s < SB; ++s)
-#pragma unroll
-        for (int k = 0; k < kRowsPerThr; ++k) acc[s][k] = 0.0f;
-    const size_t slice = (size_t)a.V * a.C;
-    if (__syncthreads_or(any)) {
-        const float *sb[SB];
-#pragma unroll
-        for (int s = 0; s < SB; ++s) sb[s] = sino + (size_t)min(b0 + s, batch - 1) * slice;
-        for (int v = 0; v < a.V; ++v) {
-            const float2 cs = __ldg(view_cs + v);
-            const size_t ro = (size_t)v * a.C;
-#pragma unroll
-            for (int k = 0; k < kRowsPerThr; ++k) {
-                const float U = fmaf(px, cs.x, fmaf(py[k], cs.y, a.R));
-                const float t = fmaf(py[k], cs.x, -px * cs.y);
-                const float rU = __fdividef(1.0f, U);
-                const float g = fov_atan<DEG>(t * rU, a.coef);
-                const float y = fmaf(g, a.inv_dcol, a.pos_off);
-                if (in[k] && y > 0.5f && y < a.fC + 0.5f) {
-                    int i;
-                    float f;
-                    split_pos(y, i, f);
-                    const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
-                    float wgt = 1.0f;
-                    if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));
-#pragma unroll
-                    for (int s = 0; s < SB; ++s) {
-                        const float v0 = __ldg(sb[s] + ro + i0), v1 = __ldg(sb[s] + ro + i1);
-                        const float val = fmaf(f, v1 - v0, v0);
-                        acc[s][k] = WEIGHTED ? fmaf(val, wgt, acc[s][k]) : acc[s][k] + val;
-                    }
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int s = 0; s < SB; ++s) {
-        if (b0 + s >= batch) break;
-        float *ib = img + (size_t)(b0 + s) * a.nx * a.ny;
-#pragma unroll
-        for (int k = 0; k < kRowsPerThr; ++k) {
-            const int iy = iy0 + 8 * k;
-            if (ix < a.nx && iy < a.ny) ib[(size_t)iy * a.nx + ix] = acc[s][k];
-        }
-    }
+    const size_t slice = (size_t)a.V * a.C, plane = (size_t)a.nx * a.ny;
+    bp_tile<WEIGHTED, SB, DEG, float>(sino + b0 * slice, slice, img + b0 * plane, plane, view_cs,
+                                      a, min(SB, batch - b0), blockIdx.x, blockIdx.y);
 }
 
 // Transpose of bp_fan_kernel: each pixel-view scatters x * weight * (1-f, f)

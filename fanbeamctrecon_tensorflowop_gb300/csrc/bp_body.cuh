@@ -1,0 +1,115 @@
+// The backprojector's per-tile work, shared by the per-plan kernel and the
+// uneven-batch kernel (geometry and arithmetic are described in bp.cu).
+#pragma once
+
+#include "fp_body.cuh"
+
+namespace ctk {
+
+constexpr int kBpTile = 32;       // tile edge (pixels)
+constexpr int kBpRowsPerThr = 4;  // 32x8 threads cover 32x32 pixels
+
+struct BpArgs {
+    int V, C, nx, ny;
+    float xmin, ymin, dx, dy;
+    float R;
+    float inv_dcol;   // 1/dcol
+    float pos_off;    // shift - left/dcol + 1/2: y = atan*inv_dcol + pos_off = col + 1/2
+    float fC;         // n_cols
+    double fov_r2;
+    float coef[9];    // atan(z) = z * sum coef[k] z^(2k) (zero-padded to degree 8)
+};
+
+template <int DEG>
+__device__ __forceinline__ float fov_atan(float z, const float *c) {
+    if constexpr (DEG == 0) {
+        return atanf(z);
+    } else {
+        const float s = z * z;
+        float p = c[DEG];
+#pragma unroll
+        for (int k = DEG - 1; k >= 0; --k) p = fmaf(p, s, c[k]);
+        return z * p;
+    }
+}
+
+// y = col + 1/2 >= 0: i = trunc(y) = floor(col - 1/2) + 1 and f = frac(y),
+// without float-to-int conversion instructions (valid for 0 <= y < 2^22).
+__device__ __forceinline__ void split_pos(float y, int &i, float &f) {
+    const float m = __fadd_rz(y, 12582912.0f);
+    i = __float_as_int(m) - 0x4B400000;
+    f = y - (m - 12582912.0f);
+}
+
+// One 32x32 tile (tx, ty) of nsl <= SB slices: sino slice s at
+// sino + s * sstride ([V][C]), image slice s at img + s * istride ([ny][nx]).
+// Block of 32 x 8 threads, four pixels per thread; block-uniform call.
+template <bool WEIGHTED, int SB, int DEG, typename OutT>
+__device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t sstride,
+                                        OutT *__restrict__ img, size_t istride,
+                                        const float2 *__restrict__ view_cs, const BpArgs &a,
+                                        int nsl, int tx, int ty) {
+    const int ix = tx * kBpTile + threadIdx.x;
+    const int iy0 = ty * kBpTile + threadIdx.y;
+    float py[kBpRowsPerThr];
+    bool in[kBpRowsPerThr];
+    const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
+    const float px = (float)xd;
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < kBpRowsPerThr; ++k) {
+        const int iy = iy0 + 8 * k;
+        const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
+        py[k] = (float)yd;
+        in[k] = ix < a.nx && iy < a.ny && (xd * xd + yd * yd <= a.fov_r2);
+        any |= in[k];
+    }
+    float acc[SB][kBpRowsPerThr];
+#pragma unroll
+    for (int s = 0; s < SB; ++s)
+#pragma unroll
+        for (int k = 0; k < kBpRowsPerThr; ++k) acc[s][k] = 0.0f;
+    if (__syncthreads_or(any)) {
+        const float *sb[SB];
+#pragma unroll
+        for (int s = 0; s < SB; ++s) sb[s] = sino + (size_t)min(s, nsl - 1) * sstride;
+        for (int v = 0; v < a.V; ++v) {
+            const float2 cs = __ldg(view_cs + v);
+            const size_t ro = (size_t)v * a.C;
+#pragma unroll
+            for (int k = 0; k < kBpRowsPerThr; ++k) {
+                const float U = fmaf(px, cs.x, fmaf(py[k], cs.y, a.R));
+                const float t = fmaf(py[k], cs.x, -px * cs.y);
+                const float rU = __fdividef(1.0f, U);
+                const float g = fov_atan<DEG>(t * rU, a.coef);
+                const float y = fmaf(g, a.inv_dcol, a.pos_off);
+                if (in[k] && y > 0.5f && y < a.fC + 0.5f) {
+                    int i;
+                    float f;
+                    split_pos(y, i, f);
+                    const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
+                    float wgt = 1.0f;
+                    if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));
+#pragma unroll
+                    for (int s = 0; s < SB; ++s) {
+                        const float v0 = __ldg(sb[s] + ro + i0), v1 = __ldg(sb[s] + ro + i1);
+                        const float val = fmaf(f, v1 - v0, v0);
+                        acc[s][k] = WEIGHTED ? fmaf(val, wgt, acc[s][k]) : acc[s][k] + val;
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < SB; ++s) {
+        if (s >= nsl) break;
+        OutT *ib = img + (size_t)s * istride;
+#pragma unroll
+        for (int k = 0; k < kBpRowsPerThr; ++k) {
+            const int iy = iy0 + 8 * k;
+            if (ix < a.nx && iy < a.ny) store_val(ib + (size_t)iy * a.nx + ix, acc[s][k]);
+        }
+    }
+}
+
+}  // namespace ctk

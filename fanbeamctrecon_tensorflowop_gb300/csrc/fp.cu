@@ -1,16 +1,13 @@
 // Ray-driven fan-beam forward projector and its exact transpose.
 //
 // Forward (replaces FP/transform.cu:103-146 and the per-view launch loop
-// :162-169): one thread per ray, all views and slices in one launch.  The
-// thread walks the bilinear cells its ray crosses and adds each cell's
-// samples in closed form (cellwalk.cuh), so the image is read once per cell
-// instead of four times per sample; SB slices share one walk.  Output:
+// :162-169): all views and slices in one launch.  Each launch first builds
+// "quad images" (per slice and layout, a float4 of the four clamped bilinear
+// taps of every cell), then fp_warp (fp_body.cuh) walks 32 adjacent rays of a
+// view per warp, row-synchronously, summing each cell's samples in closed
+// form (cellwalk.cuh): one 16-byte gather per cell instead of four per
+// sample.  Eight slices share one walk.  Output:
 // p = 0.125*dx * sum_k bilinear_clamp(img, start + k*step), k < n.
-// The lanes of a warp are adjacent rays of one view.  A ray running mostly
-// along x reads a transposed copy of the image (built per launch in the
-// workspace), so that for every view the lanes' taps lie along memory rows
-// and a warp's gather touches one or two cache lines per tap, not one line
-// per lane.
 //
 // Transpose: the image is cut into bands of 4 rows (for rays running mostly
 // along y) or 4 columns (rays mostly along x), each held with 8 slices in
@@ -25,6 +22,7 @@
 #include <climits>
 
 #include "cellwalk.cuh"
+#include "fp_body.cuh"
 
 namespace ctk {
 namespace {
@@ -47,153 +45,31 @@ constexpr int kAdjSlices = CT_ADJ_SLICES;  // slices per adjoint walk
 #endif
 constexpr int kAdjBand = CT_ADJ_BAND;  // rows (columns) per adjoint band
 
-// Quad images: for every bilinear cell (cu, cv) of the walked layout, the
-// four clamp-to-edge taps (cu,cv), (cu+1,cv), (cu,cv+1), (cu+1,cv+1) as one
-// float4, so a cell's gather is a single 16-byte load.  Samples lie inside
-// the FOV circle of radius nx/2 texels, so cells run over [-1, nx-1] in both
-// axes of both layouts; quad (qi, qj) holds cell (qi-1, qj-1) and a layout
-// is (nx+1)^2 quads.  Layout 0 walks (u, v) = (x, y); layout 1 walks the
-// transposed image, (u, v) = (y, x).
+// Builds both quad layouts of nz slices (grid.z = 2 * slices).
 __global__ void __launch_bounds__(256)
     build_quads_kernel(const float *__restrict__ img, float4 *__restrict__ quads, int nx, int ny) {
     const int Q = nx + 1;
     const int qi = blockIdx.x * 32 + threadIdx.x, qj = blockIdx.y * 8 + threadIdx.y;
     if (qi >= Q || qj >= Q) return;
     const int layout = blockIdx.z & 1, b = blockIdx.z >> 1;
-    const float *im = img + (size_t)b * nx * ny;
-    const int cu = qi - 1, cv = qj - 1;
-    // tap (du, dv) of the cell is image pixel x = cu+du, y = cv+dv (layout 0)
-    // or x = cv+dv, y = cu+du (layout 1), clamped to the image
-    float4 t;
-    float *tv = &t.x;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int du = k & 1, dv = k >> 1;
-        int x = layout ? cv + dv : cu + du;
-        int y = layout ? cu + du : cv + dv;
-        x = min(max(x, 0), nx - 1);
-        y = min(max(y, 0), ny - 1);
-        tv[k] = __ldg(im + (size_t)y * nx + x);
-    }
-    quads[((size_t)b * 2 + layout) * Q * Q + (size_t)qj * Q + qi] = t;
+    build_quad(img + (size_t)b * nx * ny,
+               quads + ((size_t)b * 2 + layout) * Q * Q + (size_t)qj * Q + qi, nx, ny, layout,
+               qi, qj);
 }
 
-template <int SB>
-struct Taps {
-    const float4 *q;  // this warp's layout of slice b0; slice s adds s * stride
-    size_t stride;    // quads between consecutive slices
-    int Q;            // quads per row (nx + 1)
-    float acc[SB];
-    __device__ __forceinline__ void add(const CellWeights &cw, int cu, int cv) {
-        const int qi = min(max(cu + 1, 0), Q - 1), qj = min(max(cv + 1, 0), Q - 1);
-        const float4 *p = q + (size_t)qj * Q + qi;
-#pragma unroll
-        for (int s = 0; s < SB; ++s) {
-            const float4 t = __ldg(p + s * stride);
-            float v = cw.w00 * t.x;
-            v = fmaf(cw.w10, t.y, v);
-            v = fmaf(cw.w01, t.z, v);
-            v = fmaf(cw.w11, t.w, v);
-            acc[s] += v;
-        }
-    }
-};
-
-// One warp = 32 consecutive channels of one view (warps never straddle views;
-// wpv warps per view).  The warp votes its layout (transposed when most rays
-// run along x) and its row direction, then steps through the rows of that
-// layout in lockstep: in each row every lane sums the (one to three) cells its
-// ray crosses there.  Lanes therefore gather from the same one or two rows at
-// a time, whatever depth their rays entered the FOV at.  A lane whose ray
-// runs against the warp's direction (possible only at a layout boundary)
-// walks on its own afterwards.
 template <int SB>
 __global__ void __launch_bounds__(kFpThreads, CT_FP_MIN_BLOCKS)
     fp_fan_kernel(const float4 *__restrict__ quads, float *__restrict__ sino,
                   const float4 *__restrict__ ray, const int *__restrict__ nsamp, int V, int C,
                   int wpv, int nx, float w, int batch, int max_iter) {
-    constexpr unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * (kFpThreads / 32) + (threadIdx.x >> 5);
     if (gw >= V * wpv) return;  // warp-uniform
-    const int v = gw / wpv;
-    const int c = (gw - v * wpv) * 32 + lane;
-    const bool has_c = c < C;
-    const int r = v * C + (has_c ? c : C - 1);
     const int b0 = blockIdx.y * SB;
-    const int n = has_c ? __ldg(nsamp + r) : 0;
-    const bool valid = n > 0;
-    const float4 q = valid ? __ldg(ray + r) : make_float4(0.f, 0.f, 0.f, 0.f);
-
-    const unsigned vm = __ballot_sync(FULL, valid);
-    const unsigned xm = __ballot_sync(FULL, valid && fabsf(q.z) > fabsf(q.w));
-    const bool along_x = 2 * __popc(xm) > __popc(vm);
-    const RaySeg seg = along_x ? RaySeg{q.y - 0.5f, q.x - 0.5f, q.w, q.z}
-                               : RaySeg{q.x - 0.5f, q.y - 0.5f, q.z, q.w};
-    Taps<SB> tp;
-    tp.Q = nx + 1;
-    const size_t lsz = (size_t)tp.Q * tp.Q;
-    tp.stride = 2 * lsz;
-    // slices beyond the batch read the last slice's quads (results dropped)
-    tp.q = quads + (size_t)b0 * tp.stride + (along_x ? lsz : 0);
-#pragma unroll
-    for (int s = 0; s < SB; ++s) tp.acc[s] = 0.0f;
-    const unsigned pm = __ballot_sync(FULL, valid && seg.sv > 0.0f);
-    const int dir = 2 * __popc(pm) >= __popc(vm) ? 1 : -1;
-    const bool synced = valid && (dir > 0 ? seg.sv > 0.0f : seg.sv < 0.0f);
-    const float nf = (float)n;
-    // rows of the first and last sample, one row of slack on each side
-    const int jf = (int)floorf(seg.v0);
-    const int jl = (int)floorf(fmaf(seg.sv, nf - 1.0f, seg.v0));
-    int J0, J1;
-    if (dir > 0) {
-        J0 = __reduce_min_sync(FULL, synced ? jf : INT_MAX) - 1;
-        J1 = __reduce_max_sync(FULL, synced ? jl : INT_MIN) + 1;
-    } else {
-        J0 = __reduce_max_sync(FULL, synced ? jf : INT_MIN) + 1;
-        J1 = __reduce_min_sync(FULL, synced ? jl : INT_MAX) - 1;
-    }
-    if (__any_sync(FULL, synced)) {
-        const float INF = __int_as_float(0x7f800000);
-        const float iu = seg.su != 0.0f ? 1.0f / seg.su : 0.0f;
-        const float iv = synced ? 1.0f / seg.sv : 0.0f;
-        const float du = seg.su >= 0.0f ? 1.0f : -1.0f;
-        const int rows = (J1 - J0) * dir + 1;
-        for (int it = 0; it < rows; ++it) {
-            const int j = J0 + it * dir;
-            if (!synced) continue;
-            const float tA = ((float)j - seg.v0) * iv, tB = ((float)(j + 1) - seg.v0) * iv;
-            const float ka = fmaxf(0.0f, ceilf(fminf(tA, tB)));
-            const float kb = fminf(nf, ceilf(fmaxf(tA, tB)));
-            if (!(ka < kb)) continue;
-            float cu = floorf(fmaf(seg.su, ka, seg.u0));
-            float bu = seg.su >= 0.0f ? cu + 1.0f : cu;
-            float k = ka;
-            for (int t = 0; t < 8 && k < kb; ++t) {
-                const float tu = seg.su != 0.0f ? (bu - seg.u0) * iu : INF;
-                const float ke = fminf(kb, ceilf(tu));
-                const float cnt = ke - k;
-                if (cnt > 0.0f) {
-                    const float a = fmaf(seg.su, k, seg.u0) - cu;
-                    const float b = fmaf(seg.sv, k, seg.v0) - (float)j;
-                    tp.add(cell_weights(cnt, a, b, seg.su, seg.sv), (int)cu, j);
-                    k = ke;
-                }
-                cu += du;
-                bu += du;
-            }
-        }
-    }
-    if (valid && !synced) {
-        walk_cells(seg, 0.0f, nf, max_iter, [&](int cu, int cv, float cnt, float a, float b) {
-            tp.add(cell_weights(cnt, a, b, seg.su, seg.sv), cu, cv);
-        });
-    }
-    if (has_c) {
-#pragma unroll
-        for (int s = 0; s < SB; ++s)
-            if (b0 + s < batch) sino[((size_t)(b0 + s) * V + v) * C + c] = tp.acc[s] * w;
-    }
+    const size_t lsz = (size_t)(nx + 1) * (nx + 1);
+    // slices beyond the batch read slice b0's quads (results dropped)
+    fp_warp<SB, float>(quads + (size_t)b0 * 2 * lsz, 2 * lsz, sino + (size_t)b0 * V * C,
+                       (size_t)V * C, ray, nsamp, V, C, wpv, nx, w, min(SB, batch - b0),
+                       max_iter, gw);
 }
 
 // ---- transpose ----------------------------------------------------------------

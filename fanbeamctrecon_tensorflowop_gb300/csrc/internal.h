@@ -90,6 +90,8 @@ int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *st
 int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream);
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work, void *stream);
 size_t cone_fp_work_bytes(const ct_plan *p, int batch);
+ct_status batch_workspace(const ct_batch_item *items, int n, size_t *bytes);
+int batch_run(const ct_batch_item *items, int n, void *work, void *stream);
 int plain_fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *stream);
 int plain_fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
 int plain_bp_fan(const ct_plan *p, const float *sino, float *img, int batch, void *stream);

@@ -274,6 +274,44 @@ ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_
 ct_status ct_fp_cone(const ct_plan *plan, const float *d_vol, float *d_proj, int batch,
                      void *d_work, size_t work_bytes, ct_stream stream);
 
+/* ---- uneven batches ---------------------------------------------------------- */
+
+/* Element type of an operator's input and output storage; arithmetic is FP32. */
+typedef enum ct_dtype {
+    CT_DTYPE_F32 = 0,
+    CT_DTYPE_BF16 = 1 /* bfloat16 storage, FP32 accumulation */
+} ct_dtype;
+
+#define CT_BATCH_MAX_ITEMS 64
+
+/* One slice of an uneven batch: a fan-beam plan (any geometry; plans made by
+ * ct_plan_create), one of CT_OP_FP, CT_OP_BP, CT_OP_FBP, CT_OP_FBP_ADJOINT,
+ * the storage type of d_in and d_out, and device pointers to one input slice
+ * (image [ny][nx] or sinogram [n_views][n_cols]) and one output slice. */
+typedef struct ct_batch_item {
+    const ct_plan *plan;
+    int32_t op;
+    int32_t dtype;
+    const void *d_in;
+    void *d_out;
+} ct_batch_item;
+
+/* Device scratch bytes ct_batch_run needs for these items. */
+ct_status ct_batch_workspace_size(const ct_batch_item *items, int n, size_t *bytes);
+
+/* Runs up to CT_BATCH_MAX_ITEMS slices of different geometries and
+ * operators: one launch builds every FP item's quad images, one persistent
+ * launch projects all FP items, the FBP / FBP-adjoint items are filtered with
+ * their plans' filters, and one persistent launch backprojects all BP / FBP
+ * items.  Item descriptors are passed as kernel parameters, so the call makes
+ * no host-to-device copy and can be captured in a CUDA graph (pass d_work; the
+ * first call of a process should come before capture).  All plans must be on
+ * one device.  d_work == NULL allocates stream-ordered, as the operators do.
+ * No counterpart in the reference (one op instance per geometry, one slice
+ * loop per call). */
+ct_status ct_batch_run(const ct_batch_item *items, int n, void *d_work, size_t work_bytes,
+                       ct_stream stream);
+
 /* ---- filtered backprojection that allocates nothing ----------------------- */
 
 /* Capacity, in floats, of the fixed device array ct_fbp_fan_static_scratch

@@ -72,3 +72,18 @@ def config4(views=984, cols=888, n_rows=64, nz=64, n=512):
     p = fan_param16(sdd=SDD, sid=SID, n_views=views, n_cols=cols, n=n, pixel_mm=0.7,
                     dcol_rad=DCOL, det_bottom=-n_rows / 2.0, drow=1.0, dz=0.625)
     return p, angle(views, 0.0), n_rows, nz
+
+
+UNEVEN = [(256, 492, 512), (384, 720, 736), (512, 984, 888)]
+
+
+def uneven(k, scale=1):
+    """The k-th geometry of the uneven workload (cycling image 256^2 / 384^2 /
+    512^2, views 492 / 720 / 984, channels 512 / 736 / 888), pixel pitch chosen
+    so that rFOV = 179.2 mm for every size; scale > 1 shrinks all three sizes."""
+    n, v, c = UNEVEN[k % 3]
+    n, v, c = n // scale, v // scale, c // scale // 4 * 4
+    pix = 358.4 / n
+    dcol = DCOL * (888 / c) if scale > 1 else DCOL
+    p = fan_param16(sdd=SDD, sid=SID, n_views=v, n_cols=c, n=n, pixel_mm=pix, dcol_rad=dcol)
+    return p, angle(v, 0.0)

@@ -1,0 +1,113 @@
+"""Uneven batches (ct_batch_run): per-item results equal the per-plan
+operators, BF16 storage stays within BF16 rounding of the FP32 result, a
+captured CUDA graph replays the same results, and bad batches are refused."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from fanbeamctrecon_tensorflowop_gb300 import _lib, phantom
+from fanbeamctrecon_tensorflowop_gb300.batch import UnevenBatch
+from fanbeamctrecon_tensorflowop_gb300.ops import ConePlan, FanPlan
+import geometries as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _tol(op):
+    # the FBP adjoint's weighted-BP transpose adds with float atomics, so its
+    # summation order (and last bits) vary from run to run
+    return 1e-5 if op == "fbp_adjoint" else 1e-6
+
+
+def _np(t):
+    torch.cuda.synchronize()
+    return t.detach().float().cpu().numpy().astype(np.float64)
+
+
+def _make(cuda, dtype, ops=("fp", "fbp", "fbp_adjoint", "bp"), n_items=8, scale=4):
+    items, ref = [], []
+    for k in range(n_items):
+        p, a = G.uneven(k, scale=scale)
+        plan = FanPlan(p, a, device=cuda)
+        op = ops[k % len(ops)]
+        g = plan.geom
+        img = torch.from_numpy(phantom.ellipse_phantom(g.nx, float(g.dx), seed=k)).to(cuda)
+        sino = plan.fp(img)[0]
+        x = img if op in ("fp", "fbp_adjoint") else sino
+        x = x.to(dtype).contiguous()
+        out_shape = plan.sino_shape if op in ("fp", "fbp_adjoint") else plan.image_shape
+        y = torch.full(out_shape, float("nan"), device=cuda, dtype=dtype)
+        items.append((plan, op, x, y))
+        xf = x.float()
+        want = {"fp": plan.fp, "bp": plan.bp, "fbp": plan.fbp,
+                "fbp_adjoint": plan.fbp_adjoint}[op](xf)[0]
+        ref.append(want)
+    return items, ref
+
+
+def test_batch_f32_equals_per_plan_operators(cuda):
+    items, ref = _make(cuda, torch.float32)
+    UnevenBatch(items).run()
+    for (plan, op, x, y), want in zip(items, ref):
+        assert rel_l2(_np(y), _np(want)) <= _tol(op), op
+
+
+def test_batch_bf16_storage(cuda, orc):
+    items, ref = _make(cuda, torch.bfloat16)
+    UnevenBatch(items).run()
+    for (plan, op, x, y), want in zip(items, ref):
+        # FP32 arithmetic on the BF16 input: only the output rounding differs
+        assert rel_l2(_np(y), _np(want)) <= 8e-3, op
+    # errors against the FP64 oracle of the BF16-rounded inputs
+    for (plan, op, x, y), _ in zip(items[:4], ref[:4]):
+        g = orc.decode(plan.param16)
+        xin = _np(x)
+        o = {"fp": lambda: orc.fp_fan(g, plan.angles, xin),
+             "fbp": lambda: orc.fbp_fan(g, plan.angles, xin),
+             "fbp_adjoint": lambda: orc.fbp_fan_adjoint(g, plan.angles, xin),
+             "bp": lambda: orc.bp_fan(g, plan.angles, xin)}[op]()[0]
+        assert rel_l2(_np(y), o) <= 8e-3, op
+
+
+def test_batch_graph_replay(cuda):
+    items, ref = _make(cuda, torch.float32, n_items=6)
+    ub = UnevenBatch(items)
+    ub.capture()
+    for _, _, _, y in items:
+        y.fill_(float("nan"))
+    ub.replay()
+    for (plan, op, x, y), want in zip(items, ref):
+        assert rel_l2(_np(y), _np(want)) <= _tol(op), op
+    # new inputs, same buffers: the graph recomputes
+    for _, op, x, _ in items:
+        x.mul_(2.0)
+    ub.replay()
+    for (plan, op, x, y), want in zip(items, ref):
+        assert rel_l2(_np(y), 2.0 * _np(want)) <= _tol(op), op
+
+
+def test_batch_validation(cuda):
+    items, _ = _make(cuda, torch.float32, n_items=2)
+    lib = _lib.load()
+    arr = (_lib.CtBatchItem * 65)()
+    n = __import__("ctypes").c_size_t()
+    assert lib.ct_batch_workspace_size(arr, 65, n) == 1
+    bad = (_lib.CtBatchItem * 1)()
+    bad[0].plan = items[0][0]._h.value
+    bad[0].op = 99
+    bad[0].d_in, bad[0].d_out = items[0][2].data_ptr(), items[0][3].data_ptr()
+    assert lib.ct_batch_workspace_size(bad, 1, n) == 1
+    bad[0].op = _lib.OP_FP
+    bad[0].d_in = None
+    assert lib.ct_batch_workspace_size(bad, 1, n) == 2
+    p, a, nr, nz = G.cone_small()
+    cone = ConePlan(p, a, nr, nz, device=cuda)
+    with pytest.raises(TypeError):
+        UnevenBatch([(cone, "fp", torch.zeros(nz, 32, 32, device=cuda),
+                      torch.zeros(48, 64, device=cuda))])
+    with pytest.raises(TypeError):
+        plan, op, x, y = items[0]
+        UnevenBatch([(plan, op, x.to(torch.bfloat16), y)])
