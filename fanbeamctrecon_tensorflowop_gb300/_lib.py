@@ -71,7 +71,7 @@ BATCH_MAX_ITEMS = 64
 
 class CtPlanOpts(ctypes.Structure):
     _fields_ = [("filter_window", ctypes.c_int32), ("filter_algo", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("short_scan", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
 _vp = ctypes.c_void_p

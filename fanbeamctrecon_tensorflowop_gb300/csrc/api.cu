@@ -82,18 +82,19 @@ size_t proj_bytes(const ct_plan *p, int batch) {
 }
 
 size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
+    const size_t parker = p->d_parker ? 2 : 1;  // weighted copy + filtered copy
     switch (op) {
         case CT_OP_FP_CONE:
             return ctk::cone_fp_work_bytes(p, batch);
         case CT_OP_FDK_CONE:
         case CT_OP_FDK_CONE_ADJOINT:
-            return proj_bytes(p, batch);
+            return parker * proj_bytes(p, batch);
         case CT_OP_FP:
             return ctk::fp_fan_work_bytes(p, batch);
         case CT_OP_FBP:
         case CT_OP_FBP_ADJOINT:
         case CT_OP_FDK_BP:
-            return sino_bytes(p, batch);
+            return parker * sino_bytes(p, batch);
         default:
             return 0;
     }
@@ -109,6 +110,7 @@ void free_plan(ct_plan *p) {
     cudaFree(p->d_tc_hi);
     cudaFree(p->d_tc_lo);
     cudaFree(p->d_err);
+    cudaFree(p->d_parker);
     delete p;
 }
 
@@ -126,10 +128,17 @@ ct_status upload(T **dst, const std::vector<T> &src) {
 ct_status filtered_bp(const ct_plan *p, const float *d_sino, float *d_img, int batch,
                       void *d_work, size_t work_bytes, cudaStream_t s, const char *name) {
     Workspace w;
-    ct_status st = acquire(w, d_work, work_bytes, sino_bytes(p, batch), s);
+    ct_status st = acquire(w, d_work, work_bytes, op_workspace(p, CT_OP_FBP, batch), s);
     if (st != CT_OK) return st;
     float *filt = static_cast<float *>(w.ptr);
-    st = launch_status(ctk::ramp_filter(p, d_sino, filt, batch * p->g.n_views, s), name);
+    const float *src = d_sino;
+    if (p->d_parker) {  // short scan: weight, then filter
+        float *wtd = filt + (size_t)batch * p->g.n_views * p->g.n_cols;
+        st = launch_status(ctk::apply_parker(p, d_sino, wtd, batch, s), name);
+        if (st != CT_OK) return st;
+        src = wtd;
+    }
+    st = launch_status(ctk::ramp_filter(p, src, filt, batch * p->g.n_views, s), name);
     if (st != CT_OK) return st;
     return launch_status(ctk::bp_fan(p, filt, d_img, batch, 1, s), name);
 }
@@ -198,6 +207,7 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
         o = *opts;
         for (int r : o.reserved)
             if (r != 0) return CT_ERR_INVALID_ARGUMENT;
+        if (o.short_scan != 0 && o.short_scan != 1) return CT_ERR_INVALID_ARGUMENT;
     }
     if (o.filter_window != CT_WINDOW_RAMLAK && o.filter_window != CT_WINDOW_SHEPP_LOGAN)
         return CT_ERR_INVALID_ARGUMENT;
@@ -211,6 +221,7 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
     ct_build_ray_table(geom, angles, &t);
     ct_build_filter_taps(geom, o.filter_window, &t);
     ct_build_channel_table(geom, &t);
+    if (o.short_scan) ct_build_parker(geom, angles, &t);
 
     ct_plan *p = new (std::nothrow) ct_plan();
     if (!p) return CT_ERR_ALLOC;
@@ -238,7 +249,8 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
     if ((st = upload(&p->d_view_cs, t.view_cs)) != CT_OK ||
         (st = upload(&p->d_ray, t.ray)) != CT_OK || (st = upload(&p->d_nsamp, t.nsamp)) != CT_OK ||
         (st = upload(&p->d_taps, t.taps)) != CT_OK ||
-        (st = upload(&p->d_chan_s, t.chan_s)) != CT_OK) {
+        (st = upload(&p->d_chan_s, t.chan_s)) != CT_OK ||
+        (st = upload(&p->d_parker, t.parker)) != CT_OK) {
         free_plan(p);
         return st;
     }
@@ -391,14 +403,22 @@ ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_s
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     Workspace w;
-    st = acquire(w, d_work, work_bytes, sino_bytes(plan, batch), stream);
+    st = acquire(w, d_work, work_bytes, op_workspace(plan, CT_OP_FBP_ADJOINT, batch), stream);
     if (st != CT_OK) return st;
     float *tmp = static_cast<float *>(w.ptr);
     st = launch_status(ctk::bp_fan_transpose(plan, d_img, tmp, batch, 1, stream),
                        "ct_fbp_fan_adjoint");
     if (st != CT_OK) return st;
-    // The row filter is a symmetric Toeplitz matrix: its transpose is itself.
-    return launch_status(ctk::ramp_filter(plan, tmp, d_sino, batch * plan->g.n_views, stream),
+    // The row filter is a symmetric Toeplitz matrix: its transpose is itself;
+    // the short-scan weights are diagonal.
+    if (!plan->d_parker)
+        return launch_status(ctk::ramp_filter(plan, tmp, d_sino, batch * plan->g.n_views, stream),
+                             "ct_fbp_fan_adjoint");
+    float *filt = tmp + (size_t)batch * plan->g.n_views * plan->g.n_cols;
+    st = launch_status(ctk::ramp_filter(plan, tmp, filt, batch * plan->g.n_views, stream),
+                       "ct_fbp_fan_adjoint");
+    if (st != CT_OK) return st;
+    return launch_status(ctk::apply_parker(plan, filt, d_sino, batch, stream),
                          "ct_fbp_fan_adjoint");
 }
 
@@ -436,11 +456,18 @@ ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, in
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     Workspace w;
-    st = acquire(w, d_work, work_bytes, proj_bytes(plan, batch), stream);
+    st = acquire(w, d_work, work_bytes, op_workspace(plan, CT_OP_FDK_CONE, batch), stream);
     if (st != CT_OK) return st;
     float *filt = static_cast<float *>(w.ptr);
+    const float *src = d_proj;
+    if (plan->d_parker) {
+        float *wtd = filt + proj_bytes(plan, batch) / sizeof(float);
+        st = launch_status(ctk::apply_parker(plan, d_proj, wtd, batch, stream), "ct_fdk_cone");
+        if (st != CT_OK) return st;
+        src = wtd;
+    }
     st = launch_status(
-        ctk::ramp_filter(plan, d_proj, filt, batch * plan->g.n_views * plan->n_rows, stream),
+        ctk::ramp_filter(plan, src, filt, batch * plan->g.n_views * plan->n_rows, stream),
         "ct_fdk_cone");
     if (st != CT_OK) return st;
     return launch_status(ctk::cone_bp(plan, filt, d_vol, batch, stream), "ct_fdk_cone");
@@ -457,15 +484,22 @@ ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     Workspace w;
-    st = acquire(w, d_work, work_bytes, proj_bytes(plan, batch), stream);
+    st = acquire(w, d_work, work_bytes, op_workspace(plan, CT_OP_FDK_CONE_ADJOINT, batch),
+                 stream);
     if (st != CT_OK) return st;
     float *tmp = static_cast<float *>(w.ptr);
     st = launch_status(ctk::cone_bp_transpose(plan, d_vol, tmp, batch, stream),
                        "ct_fdk_cone_adjoint");
     if (st != CT_OK) return st;
-    return launch_status(
-        ctk::ramp_filter(plan, tmp, d_proj, batch * plan->g.n_views * plan->n_rows, stream),
-        "ct_fdk_cone_adjoint");
+    const int rows = batch * plan->g.n_views * plan->n_rows;
+    if (!plan->d_parker)
+        return launch_status(ctk::ramp_filter(plan, tmp, d_proj, rows, stream),
+                             "ct_fdk_cone_adjoint");
+    float *filt = tmp + proj_bytes(plan, batch) / sizeof(float);
+    st = launch_status(ctk::ramp_filter(plan, tmp, filt, rows, stream), "ct_fdk_cone_adjoint");
+    if (st != CT_OK) return st;
+    return launch_status(ctk::apply_parker(plan, filt, d_proj, batch, stream),
+                         "ct_fdk_cone_adjoint");
 }
 
 ct_status ct_fp_cone(const ct_plan *plan, const float *d_vol, float *d_proj, int batch,

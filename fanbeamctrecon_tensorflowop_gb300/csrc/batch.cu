@@ -182,7 +182,7 @@ size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 
 struct Layout {
     // byte offsets into the workspace, per item (SIZE_MAX = unused)
-    std::vector<size_t> quads, in32, filt, out32;
+    std::vector<size_t> quads, in32, filt, out32, wtd;
     size_t total = 0;
 };
 
@@ -192,6 +192,7 @@ Layout plan_layout(const ct_batch_item *items, int n) {
     L.in32.assign(n, SIZE_MAX);
     L.filt.assign(n, SIZE_MAX);
     L.out32.assign(n, SIZE_MAX);
+    L.wtd.assign(n, SIZE_MAX);
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
@@ -213,11 +214,13 @@ Layout plan_layout(const ct_batch_item *items, int n) {
             case CT_OP_FBP:
                 if (bf) L.in32[i] = take(sino);
                 L.filt[i] = take(sino);
+                if (p->d_parker) L.wtd[i] = take(sino);
                 break;
             case CT_OP_FBP_ADJOINT:
                 if (bf) L.in32[i] = take(img);
                 L.filt[i] = take(sino);
                 if (bf) L.out32[i] = take(sino);
+                if (p->d_parker) L.wtd[i] = take(sino);
                 break;
             default:
                 break;
@@ -342,7 +345,13 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
         const float *in32 = bf ? static_cast<const float *>(at(L.in32[i]))
                                : static_cast<const float *>(items[i].d_in);
         if (items[i].op == CT_OP_FBP) {
-            if ((e = (cudaError_t)ramp_filter(p, in32, static_cast<float *>(at(L.filt[i])),
+            const float *src = in32;
+            if (p->d_parker) {  // short scan: weight, then filter
+                float *w = static_cast<float *>(at(L.wtd[i]));
+                if ((e = (cudaError_t)apply_parker(p, in32, w, 1, s)) != cudaSuccess) return (int)e;
+                src = w;
+            }
+            if ((e = (cudaError_t)ramp_filter(p, src, static_cast<float *>(at(L.filt[i])),
                                               p->g.n_views, s)) != cudaSuccess)
                 return (int)e;
         } else if (items[i].op == CT_OP_FBP_ADJOINT) {
@@ -351,7 +360,11 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
                 return (int)e;
             float *dst = bf ? static_cast<float *>(at(L.out32[i]))
                             : static_cast<float *>(items[i].d_out);
-            if ((e = (cudaError_t)ramp_filter(p, t, dst, p->g.n_views, s)) != cudaSuccess)
+            float *fdst = p->d_parker ? static_cast<float *>(at(L.wtd[i])) : dst;
+            if ((e = (cudaError_t)ramp_filter(p, t, fdst, p->g.n_views, s)) != cudaSuccess)
+                return (int)e;
+            if (p->d_parker &&
+                (e = (cudaError_t)apply_parker(p, fdst, dst, 1, s)) != cudaSuccess)
                 return (int)e;
         }
     }

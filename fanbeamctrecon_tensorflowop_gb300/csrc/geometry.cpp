@@ -271,3 +271,44 @@ void ct_build_channel_table(const ct_fan_geom *g, ct_host_tables *t) {
         t->chan_s[2 * i + 1] = static_cast<float>(dx * 2.0 * std::sqrt(h));
     }
 }
+
+// Parker's short-scan weights (D. L. Parker, Med. Phys. 9(2), 1982) for the
+// ray of view v and channel i: with beta = angle[v] - angle[0] and the
+// channel's fan angle gamma = left + (i + 1/2 - shift) dcol (the angle the
+// backprojector assigns to that channel), and Gamma the half fan angle (the
+// outer edge of the outermost channel),
+//   w = sin^2(pi/4 beta/(Gamma - gamma))            0 <= beta < 2(Gamma - gamma)
+//     = 1                                           ... < pi - 2 gamma
+//     = sin^2(pi/4 (pi + 2 Gamma - beta)/(Gamma + gamma))  ... <= pi + 2 Gamma
+//     = 0                                           otherwise.
+// In this geometry the same line is measured again at (beta + pi + 2 gamma,
+// -gamma), and the two weights sum to one.  A scan whose angles decrease is
+// the mirror image: beta and gamma change sign.  Stored doubled, because the
+// ramp taps carry the 0.5 of full-scan redundancy (FBP/transform.cu:156-158).
+void ct_build_parker(const ct_fan_geom *g, const float *angles, ct_host_tables *t) {
+    const int V = g->n_views, C = g->n_cols;
+    const double pi = 3.14159265358979323846;
+    const double dcol = g->dcol;
+    const double dir = (V > 1 && angles[V - 1] < angles[0]) ? -1.0 : 1.0;
+    const double g0 = (double)g->left + (0.5 - (double)g->shift) * dcol;
+    const double g1 = (double)g->left + (C - 0.5 - (double)g->shift) * dcol;
+    const double G = std::fmax(std::fabs(g0), std::fabs(g1)) + 0.5 * dcol;
+    t->parker.assign((size_t)V * C, 0.0f);
+    for (int v = 0; v < V; ++v) {
+        const double beta = dir * ((double)angles[v] - (double)angles[0]);
+        for (int i = 0; i < C; ++i) {
+            const double gam = dir * ((double)g->left + (i + 0.5 - (double)g->shift) * dcol);
+            double w = 0.0;
+            if (beta >= 0.0 && beta < 2.0 * (G - gam)) {
+                const double s = std::sin(pi / 4.0 * beta / (G - gam));
+                w = s * s;
+            } else if (beta >= 2.0 * (G - gam) && beta < pi - 2.0 * gam) {
+                w = 1.0;
+            } else if (beta >= pi - 2.0 * gam && beta <= pi + 2.0 * G) {
+                const double s = std::sin(pi / 4.0 * (pi + 2.0 * G - beta) / (G + gam));
+                w = s * s;
+            }
+            t->parker[(size_t)v * C + i] = static_cast<float>(2.0 * w);
+        }
+    }
+}

@@ -28,6 +28,7 @@ struct ct_host_tables {
     // Per channel: in-plane distance (mm) from the source to the ray's first
     // sample, and the FOV chord length (mm) (cone-beam projector heights).
     std::vector<float> chan_s;       // [2*C]
+    std::vector<float> parker;       // [V*C] short-scan weights (x2), when requested
     int32_t max_nsamp = 0;
     double total_samples = 0;        // sum of nsamp over all rays
 };
@@ -39,6 +40,7 @@ void ct_build_view_table(const ct_fan_geom *g, const float *angles, ct_host_tabl
 void ct_build_ray_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
 void ct_build_filter_taps(const ct_fan_geom *g, int window, ct_host_tables *t);
 void ct_build_channel_table(const ct_fan_geom *g, ct_host_tables *t);
+void ct_build_parker(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
 // Largest |t/U| = tan(gamma) over the FOV disc: rfov / sqrt(R^2 - rfov^2).
 double ct_max_tan_gamma(const ct_fan_geom *g);
 // Fits atan(z) = z * sum_k coef[k] (z^2)^k on |z| <= zmax (interpolation at
@@ -67,6 +69,7 @@ struct ct_plan {
     float *d_chan_s;                 // [2C]
     float *d_tc_hi, *d_tc_lo;        // tensor-core filter: TF32 split of the Toeplitz taps
     int *d_err;                      // raised by kernels whose bounded waits gave up
+    float *d_parker;                 // [V*C] short-scan weights, or NULL (full scan)
 };
 
 // Kernel launchers (defined in the .cu files).  Each returns the launch error.
@@ -86,6 +89,8 @@ int tc_padded(int C);
 bool ramp_tc_supported(int C);
 void build_tc_taps(const float *taps, int C, std::vector<float> &hi, std::vector<float> &lo);
 int ramp_filter_tc(const ct_plan *p, const float *in, float *out, int rows, void *stream);
+// out = in * parker weights (per view and channel; rows and slices broadcast)
+int apply_parker(const ct_plan *p, const float *in, float *out, int batch, void *stream);
 int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream);
 int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream);
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work, void *stream);

@@ -32,12 +32,13 @@ class FanPlan:
     nz = 1
 
     def __init__(self, param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK,
-                 filter_algo: int = _lib.FILTER_AUTO):
+                 filter_algo: int = _lib.FILTER_AUTO, short_scan: bool = False):
         self._lib = _lib.load()
         self.param16 = np.ascontiguousarray(np.asarray(param16, dtype=np.float32)).copy()
         self.angles = np.ascontiguousarray(np.asarray(angles, dtype=np.float32)).copy()
         self.geom = decode(self.param16)
         self.window = int(window)
+        self.short_scan = bool(short_scan)
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device)
@@ -46,6 +47,7 @@ class FanPlan:
         opts = _lib.CtPlanOpts()
         opts.filter_window = int(window)
         opts.filter_algo = int(filter_algo)
+        opts.short_scan = int(self.short_scan)
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             st = self._create(opts, handle)
@@ -199,10 +201,10 @@ class ConePlan(FanPlan):
     float32 [B, n_views, n_rows, n_cols]."""
 
     def __init__(self, param16, angles, n_rows: int, nz: int, device=None,
-                 window: int = _lib.WINDOW_RAMLAK):
+                 window: int = _lib.WINDOW_RAMLAK, short_scan: bool = False):
         self.n_rows = int(n_rows)
         self.nz = int(nz)
-        super().__init__(param16, angles, device=device, window=window)
+        super().__init__(param16, angles, device=device, window=window, short_scan=short_scan)
 
     def _create(self, opts, handle) -> int:
         return self._lib.ct_plan_create_cone(
@@ -266,8 +268,9 @@ class ConePlan(FanPlan):
                           out)
 
 
-def get_plan(param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK) -> FanPlan:
-    """A cached FanPlan for (parameter, angles, device, window)."""
+def get_plan(param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK,
+             short_scan: bool = False) -> FanPlan:
+    """A cached FanPlan for (parameter, angles, device, window, short scan)."""
     p = np.ascontiguousarray(np.asarray(param16, dtype=np.float32))
     a = np.ascontiguousarray(np.asarray(angles, dtype=np.float32))
     if device is None:
@@ -275,11 +278,11 @@ def get_plan(param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK) -> 
     device = torch.device(device)
     if device.type == "cuda" and device.index is None:
         device = torch.device("cuda", torch.cuda.current_device())
-    key = (p.tobytes(), a.tobytes(), str(device), int(window))
+    key = (p.tobytes(), a.tobytes(), str(device), int(window), bool(short_scan))
     with _plan_lock:
         plan = _plan_cache.get(key)
         if plan is None:
-            plan = FanPlan(p, a, device=device, window=window)
+            plan = FanPlan(p, a, device=device, window=window, short_scan=short_scan)
             _plan_cache[key] = plan
         return plan
 

@@ -106,7 +106,12 @@ typedef enum ct_filter_algo {
 typedef struct ct_plan_opts {
     int32_t filter_window;  /* ct_filter_window */
     int32_t filter_algo;    /* ct_filter_algo   */
-    int32_t reserved[6];    /* must be zero      */
+    /* 1: short-scan data; FBP, FDK and their adjoints weight every ray with
+     * Parker's weights (Parker 1982), doubled to undo the filter's 0.5
+     * full-scan redundancy factor.  config.py:24 names ParkWeighting but no
+     * reference op reads it.  0: full scan (the reference). */
+    int32_t short_scan;
+    int32_t reserved[5];    /* must be zero      */
 } ct_plan_opts;
 
 /* Operators, for ct_workspace_size. */

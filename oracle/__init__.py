@@ -87,6 +87,9 @@ def _l():
         lib.orc_fbp_fan.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
         lib.orc_fbp_fan_adjoint.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
         lib.orc_fdk_bp.argtypes = [g, fp_, ctypes.c_int, dp, dp, ctypes.c_int]
+        lib.orc_parker_weight.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        lib.orc_parker_weight.restype = ctypes.c_double
+        lib.orc_parker_weights.argtypes = [g, fp_, dp]
         ci = ctypes.c_int
         lib.orc_cone_bp.argtypes = [g, ci, ci, fp_, dp, dp, ci]
         lib.orc_cone_bp_transpose.argtypes = [g, ci, ci, fp_, dp, dp, ci]
@@ -205,24 +208,46 @@ def ramp_filter(g, sino, window: int = RAMLAK) -> np.ndarray:
     return out
 
 
-def fbp_fan(g, angles, sino, window: int = RAMLAK) -> np.ndarray:
-    y = _batch_sino(g, sino)
+def parker_weight(beta: float, gamma: float, half_fan: float) -> float:
+    """Parker's short-scan weight of the ray (beta, gamma), undoubled."""
+    return _l().orc_parker_weight(float(beta), float(gamma), float(half_fan))
+
+
+def parker_weights(g, angles) -> np.ndarray:
+    """Doubled Parker weights [n_views, n_cols] of a short-scan plan."""
+    w = np.zeros((g.n_views, g.n_cols), np.float64)
+    _l().orc_parker_weights(ctypes.byref(g), _fptr(_angles(g, angles)), _dptr(w))
+    return w
+
+
+def _weighted(g, angles, y, short_scan):
+    """Scales each (view, channel) of y [B, V, (rows,) C] by the Parker table."""
+    if not short_scan:
+        return y
+    w = parker_weights(g, angles)
+    if y.ndim == 4:
+        w = w[:, None, :]
+    return y * w
+
+
+def fbp_fan(g, angles, sino, window: int = RAMLAK, short_scan: bool = False) -> np.ndarray:
+    y = np.ascontiguousarray(_weighted(g, angles, _batch_sino(g, sino), short_scan))
     out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
     _l().orc_fbp_fan(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(y), _dptr(out),
                      y.shape[0])
     return out
 
 
-def fbp_fan_adjoint(g, angles, img, window: int = RAMLAK) -> np.ndarray:
+def fbp_fan_adjoint(g, angles, img, window: int = RAMLAK, short_scan: bool = False) -> np.ndarray:
     x = _batch_img(g, img)
     out = np.zeros((x.shape[0], g.n_views, g.n_cols), np.float64)
     _l().orc_fbp_fan_adjoint(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(x),
                              _dptr(out), x.shape[0])
-    return out
+    return _weighted(g, angles, out, short_scan)
 
 
-def fdk_bp(g, angles, sino, window: int = RAMLAK) -> np.ndarray:
-    y = _batch_sino(g, sino)
+def fdk_bp(g, angles, sino, window: int = RAMLAK, short_scan: bool = False) -> np.ndarray:
+    y = np.ascontiguousarray(_weighted(g, angles, _batch_sino(g, sino), short_scan))
     out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
     _l().orc_fdk_bp(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(y), _dptr(out),
                     y.shape[0])
@@ -273,17 +298,19 @@ def cone_bp_transpose(g, n_rows, nz, angles, vol) -> np.ndarray:
     return out
 
 
-def fdk_cone(g, n_rows, nz, angles, proj, window: int = RAMLAK) -> np.ndarray:
-    y = _batch_proj(g, n_rows, proj)
+def fdk_cone(g, n_rows, nz, angles, proj, window: int = RAMLAK,
+             short_scan: bool = False) -> np.ndarray:
+    y = np.ascontiguousarray(_weighted(g, angles, _batch_proj(g, n_rows, proj), short_scan))
     out = np.zeros((y.shape[0], nz, g.ny, g.nx), np.float64)
     _l().orc_fdk_cone(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), window, _dptr(y),
                       _dptr(out), y.shape[0])
     return out
 
 
-def fdk_cone_adjoint(g, n_rows, nz, angles, vol, window: int = RAMLAK) -> np.ndarray:
+def fdk_cone_adjoint(g, n_rows, nz, angles, vol, window: int = RAMLAK,
+                     short_scan: bool = False) -> np.ndarray:
     x = _batch_vol(g, nz, vol)
     out = np.zeros((x.shape[0], g.n_views, n_rows, g.n_cols), np.float64)
     _l().orc_fdk_cone_adjoint(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), window,
                               _dptr(x), _dptr(out), x.shape[0])
-    return out
+    return _weighted(g, angles, out, short_scan)

@@ -374,6 +374,46 @@ void orc_ramp_filter(const orc_geom *g, int window, const double *in, double *ou
     free(taps);
 }
 
+/* Parker short-scan weight (Parker, Med. Phys. 9(2), 1982), written as the
+ * product of a rising and a falling smooth step S(u) = sin^2(pi u / 2) on
+ * [0, 1] (0 below, 1 above): w = S(beta / (2 (G - gam))) *
+ * S((pi + 2 G - beta) / (2 (G + gam))), which equals the piecewise form for
+ * fans narrower than pi and is 0 outside [0, pi + 2 G]. */
+#define ORC_PI_D 3.14159265358979323846
+
+static double orc_smooth_step(double u) {
+    if (u <= 0.0) return 0.0;
+    if (u >= 1.0) return 1.0;
+    const double s = sin(0.5 * ORC_PI_D * u);
+    return s * s;
+}
+
+double orc_parker_weight(double beta, double gam, double G) {
+    if (beta < 0.0 || beta > ORC_PI_D + 2.0 * G) return 0.0;
+    return orc_smooth_step(beta / (2.0 * (G - gam))) *
+           orc_smooth_step((ORC_PI_D + 2.0 * G - beta) / (2.0 * (G + gam)));
+}
+
+/* Doubled Parker weights per (view, channel): beta from angles[0] (mirrored
+ * for decreasing angles), gam = left + (i + 1/2 - shift) dcol, G the outer
+ * edge of the outermost channel.  The 2 undoes the 0.5 of the ramp taps. */
+void orc_parker_weights(const orc_geom *g, const float *angles, double *w) {
+    const int V = g->n_views, C = g->n_cols;
+    const double dc = g->dcol;
+    const double dir = (V > 1 && angles[V - 1] < angles[0]) ? -1.0 : 1.0;
+    double G = 0.0;
+    for (int i = 0; i < C; ++i) {
+        const double a = fabs((double)g->left + (i + 0.5 - (double)g->shift) * dc) + 0.5 * dc;
+        if (a > G) G = a;
+    }
+    for (int v = 0; v < V; ++v)
+        for (int i = 0; i < C; ++i) {
+            const double beta = dir * ((double)angles[v] - (double)angles[0]);
+            const double gam = dir * ((double)g->left + (i + 0.5 - (double)g->shift) * dc);
+            w[(size_t)v * C + i] = 2.0 * orc_parker_weight(beta, gam, G);
+        }
+}
+
 /* backproject_fan_curve of FBP/transform.cu:117-201: filter, then weighted BP. */
 void orc_fbp_fan(const orc_geom *g, const float *angles, int window, const double *sino,
                  double *img, int batch) {

@@ -87,3 +87,16 @@ def uneven(k, scale=1):
     dcol = DCOL * (888 / c) if scale > 1 else DCOL
     p = fan_param16(sdd=SDD, sid=SID, n_views=v, n_cols=c, n=n, pixel_mm=pix, dcol_rad=dcol)
     return p, angle(v, 0.0)
+
+
+def short_scan(n=128, views=200, cols=320, pixel=2.0, dcol=1.5 * DCOL, start=0.3,
+               reverse=False, shift=0.0, **kw):
+    """A short scan: views evenly over pi + 2*Gamma (Gamma = the half fan
+    angle to the outer channel edge), both ends included; parameter[3] makes
+    the decoded angle step equal the view spacing."""
+    half_fan = cols * dcol / 2.0 + abs(shift) * dcol
+    step = (math.pi + 2.0 * half_fan) / (views - 1)
+    p = fan_param16(sdd=SDD, sid=SID, n_views=views, n_cols=cols, n=n, pixel_mm=pixel,
+                    dcol_rad=dcol, full_angle=math.degrees(step * views), shift=shift, **kw)
+    a = (start + np.arange(views) * step).astype(np.float32)
+    return p, (a[::-1].copy() if reverse else a)
