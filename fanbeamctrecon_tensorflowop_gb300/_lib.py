@@ -71,7 +71,8 @@ BATCH_MAX_ITEMS = 64
 
 class CtPlanOpts(ctypes.Structure):
     _fields_ = [("filter_window", ctypes.c_int32), ("filter_algo", ctypes.c_int32),
-                ("short_scan", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("short_scan", ctypes.c_int32), ("cosine_weight", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 _vp = ctypes.c_void_p
@@ -91,6 +92,8 @@ SIGNATURES = {
     "ct_plan_create": (_i, [_P(CtFanGeom), _P(ctypes.c_float), _i, _P(CtPlanOpts), _P(_vp)]),
     "ct_plan_create_cone": (_i, [_P(CtFanGeom), _i, _i, _P(ctypes.c_float), _i, _P(CtPlanOpts),
                                  _P(_vp)]),
+    "ct_plan_create_cone_ex": (_i, [_P(CtFanGeom), _i, _i, _P(ctypes.c_float),
+                                    _P(ctypes.c_float), _i, _P(CtPlanOpts), _P(_vp)]),
     "ct_plan_destroy": (_i, [_vp]),
     "ct_plan_check": (_i, [_vp]),
     "ct_plan_geom": (_i, [_vp, _P(CtFanGeom)]),

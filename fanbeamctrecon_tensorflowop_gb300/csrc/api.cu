@@ -82,7 +82,7 @@ size_t proj_bytes(const ct_plan *p, int batch) {
 }
 
 size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
-    const size_t parker = p->d_parker ? 2 : 1;  // weighted copy + filtered copy
+    const size_t parker = ctk::has_preweight(p) ? 2 : 1;  // weighted copy + filtered copy
     switch (op) {
         case CT_OP_FP_CONE:
             return ctk::cone_fp_work_bytes(p, batch);
@@ -111,6 +111,8 @@ void free_plan(ct_plan *p) {
     cudaFree(p->d_tc_lo);
     cudaFree(p->d_err);
     cudaFree(p->d_parker);
+    cudaFree(p->d_cosw);
+    cudaFree(p->d_view_z);
     delete p;
 }
 
@@ -132,9 +134,9 @@ ct_status filtered_bp(const ct_plan *p, const float *d_sino, float *d_img, int b
     if (st != CT_OK) return st;
     float *filt = static_cast<float *>(w.ptr);
     const float *src = d_sino;
-    if (p->d_parker) {  // short scan: weight, then filter
+    if (ctk::has_preweight(p)) {  // short scan / cosine: weight, then filter
         float *wtd = filt + (size_t)batch * p->g.n_views * p->g.n_cols;
-        st = launch_status(ctk::apply_parker(p, d_sino, wtd, batch, s), name);
+        st = launch_status(ctk::apply_preweight(p, d_sino, wtd, batch, s), name);
         if (st != CT_OK) return st;
         src = wtd;
     }
@@ -188,8 +190,9 @@ ct_status ct_fp_ray_table(const ct_fan_geom *geom, const float *angles, int n_an
     return CT_OK;
 }
 
-static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const float *angles,
-                             int n_angles, const ct_plan_opts *opts, ct_plan **out) {
+static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool cone,
+                             const float *angles, const float *source_z, int n_angles,
+                             const ct_plan_opts *opts, ct_plan **out) {
     if (!geom || !angles || !out) return CT_ERR_NULL_POINTER;
     *out = nullptr;
     ct_status st = ct_validate_geom(geom);
@@ -200,7 +203,8 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
         return CT_ERR_INVALID_ARGUMENT;
     if (n_angles != geom->n_views) return CT_ERR_INVALID_ARGUMENT;
     for (int v = 0; v < n_angles; ++v)
-        if (!std::isfinite(angles[v])) return CT_ERR_INVALID_ARGUMENT;
+        if (!std::isfinite(angles[v]) || (source_z && !std::isfinite(source_z[v])))
+            return CT_ERR_INVALID_ARGUMENT;
     ct_plan_opts o;
     std::memset(&o, 0, sizeof(o));
     if (opts) {
@@ -208,6 +212,7 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
         for (int r : o.reserved)
             if (r != 0) return CT_ERR_INVALID_ARGUMENT;
         if (o.short_scan != 0 && o.short_scan != 1) return CT_ERR_INVALID_ARGUMENT;
+        if (o.cosine_weight != 0 && o.cosine_weight != 1) return CT_ERR_INVALID_ARGUMENT;
     }
     if (o.filter_window != CT_WINDOW_RAMLAK && o.filter_window != CT_WINDOW_SHEPP_LOGAN)
         return CT_ERR_INVALID_ARGUMENT;
@@ -222,6 +227,8 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
     ct_build_filter_taps(geom, o.filter_window, &t);
     ct_build_channel_table(geom, &t);
     if (o.short_scan) ct_build_parker(geom, angles, &t);
+    if (o.cosine_weight) ct_build_cosine(geom, n_rows, cone, &t);
+    if (source_z) t.view_z.assign(source_z, source_z + n_angles);
 
     ct_plan *p = new (std::nothrow) ct_plan();
     if (!p) return CT_ERR_ALLOC;
@@ -250,7 +257,9 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
         (st = upload(&p->d_ray, t.ray)) != CT_OK || (st = upload(&p->d_nsamp, t.nsamp)) != CT_OK ||
         (st = upload(&p->d_taps, t.taps)) != CT_OK ||
         (st = upload(&p->d_chan_s, t.chan_s)) != CT_OK ||
-        (st = upload(&p->d_parker, t.parker)) != CT_OK) {
+        (st = upload(&p->d_parker, t.parker)) != CT_OK ||
+        (st = upload(&p->d_cosw, t.cosw)) != CT_OK ||
+        (st = upload(&p->d_view_z, t.view_z)) != CT_OK) {
         free_plan(p);
         return st;
     }
@@ -275,15 +284,21 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, const 
 
 ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_angles,
                          const ct_plan_opts *opts, ct_plan **out) {
-    return plan_create(geom, 1, 1, angles, n_angles, opts, out);
+    return plan_create(geom, 1, 1, false, angles, nullptr, n_angles, opts, out);
+}
+
+ct_status ct_plan_create_cone_ex(const ct_fan_geom *geom, int n_rows, int nz,
+                                 const float *angles, const float *source_z, int n_angles,
+                                 const ct_plan_opts *opts, ct_plan **out) {
+    if (!geom) return CT_ERR_NULL_POINTER;
+    if (!(geom->drow > 0.0f) || !(geom->dz > 0.0f) || !(geom->sdd > geom->sid))
+        return CT_ERR_INVALID_ARGUMENT;
+    return plan_create(geom, n_rows, nz, true, angles, source_z, n_angles, opts, out);
 }
 
 ct_status ct_plan_create_cone(const ct_fan_geom *geom, int n_rows, int nz, const float *angles,
                               int n_angles, const ct_plan_opts *opts, ct_plan **out) {
-    if (!geom) return CT_ERR_NULL_POINTER;
-    if (!(geom->drow > 0.0f) || !(geom->dz > 0.0f) || !(geom->sdd > geom->sid))
-        return CT_ERR_INVALID_ARGUMENT;
-    return plan_create(geom, n_rows, nz, angles, n_angles, opts, out);
+    return ct_plan_create_cone_ex(geom, n_rows, nz, angles, nullptr, n_angles, opts, out);
 }
 
 ct_status ct_plan_destroy(ct_plan *plan) {
@@ -411,14 +426,14 @@ ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_s
     if (st != CT_OK) return st;
     // The row filter is a symmetric Toeplitz matrix: its transpose is itself;
     // the short-scan weights are diagonal.
-    if (!plan->d_parker)
+    if (!ctk::has_preweight(plan))
         return launch_status(ctk::ramp_filter(plan, tmp, d_sino, batch * plan->g.n_views, stream),
                              "ct_fbp_fan_adjoint");
     float *filt = tmp + (size_t)batch * plan->g.n_views * plan->g.n_cols;
     st = launch_status(ctk::ramp_filter(plan, tmp, filt, batch * plan->g.n_views, stream),
                        "ct_fbp_fan_adjoint");
     if (st != CT_OK) return st;
-    return launch_status(ctk::apply_parker(plan, filt, d_sino, batch, stream),
+    return launch_status(ctk::apply_preweight(plan, filt, d_sino, batch, stream),
                          "ct_fbp_fan_adjoint");
 }
 
@@ -460,9 +475,9 @@ ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, in
     if (st != CT_OK) return st;
     float *filt = static_cast<float *>(w.ptr);
     const float *src = d_proj;
-    if (plan->d_parker) {
+    if (ctk::has_preweight(plan)) {
         float *wtd = filt + proj_bytes(plan, batch) / sizeof(float);
-        st = launch_status(ctk::apply_parker(plan, d_proj, wtd, batch, stream), "ct_fdk_cone");
+        st = launch_status(ctk::apply_preweight(plan, d_proj, wtd, batch, stream), "ct_fdk_cone");
         if (st != CT_OK) return st;
         src = wtd;
     }
@@ -492,13 +507,13 @@ ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_
                        "ct_fdk_cone_adjoint");
     if (st != CT_OK) return st;
     const int rows = batch * plan->g.n_views * plan->n_rows;
-    if (!plan->d_parker)
+    if (!ctk::has_preweight(plan))
         return launch_status(ctk::ramp_filter(plan, tmp, d_proj, rows, stream),
                              "ct_fdk_cone_adjoint");
     float *filt = tmp + proj_bytes(plan, batch) / sizeof(float);
     st = launch_status(ctk::ramp_filter(plan, tmp, filt, rows, stream), "ct_fdk_cone_adjoint");
     if (st != CT_OK) return st;
-    return launch_status(ctk::apply_parker(plan, filt, d_proj, batch, stream),
+    return launch_status(ctk::apply_preweight(plan, filt, d_proj, batch, stream),
                          "ct_fdk_cone_adjoint");
 }
 

@@ -214,13 +214,13 @@ Layout plan_layout(const ct_batch_item *items, int n) {
             case CT_OP_FBP:
                 if (bf) L.in32[i] = take(sino);
                 L.filt[i] = take(sino);
-                if (p->d_parker) L.wtd[i] = take(sino);
+                if (has_preweight(p)) L.wtd[i] = take(sino);
                 break;
             case CT_OP_FBP_ADJOINT:
                 if (bf) L.in32[i] = take(img);
                 L.filt[i] = take(sino);
                 if (bf) L.out32[i] = take(sino);
-                if (p->d_parker) L.wtd[i] = take(sino);
+                if (has_preweight(p)) L.wtd[i] = take(sino);
                 break;
             default:
                 break;
@@ -346,9 +346,9 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
                                : static_cast<const float *>(items[i].d_in);
         if (items[i].op == CT_OP_FBP) {
             const float *src = in32;
-            if (p->d_parker) {  // short scan: weight, then filter
+            if (has_preweight(p)) {  // short scan / cosine: weight, then filter
                 float *w = static_cast<float *>(at(L.wtd[i]));
-                if ((e = (cudaError_t)apply_parker(p, in32, w, 1, s)) != cudaSuccess) return (int)e;
+                if ((e = (cudaError_t)apply_preweight(p, in32, w, 1, s)) != cudaSuccess) return (int)e;
                 src = w;
             }
             if ((e = (cudaError_t)ramp_filter(p, src, static_cast<float *>(at(L.filt[i])),
@@ -360,11 +360,11 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
                 return (int)e;
             float *dst = bf ? static_cast<float *>(at(L.out32[i]))
                             : static_cast<float *>(items[i].d_out);
-            float *fdst = p->d_parker ? static_cast<float *>(at(L.wtd[i])) : dst;
+            float *fdst = has_preweight(p) ? static_cast<float *>(at(L.wtd[i])) : dst;
             if ((e = (cudaError_t)ramp_filter(p, t, fdst, p->g.n_views, s)) != cudaSuccess)
                 return (int)e;
-            if (p->d_parker &&
-                (e = (cudaError_t)apply_parker(p, fdst, dst, 1, s)) != cudaSuccess)
+            if (has_preweight(p) &&
+                (e = (cudaError_t)apply_preweight(p, fdst, dst, 1, s)) != cudaSuccess)
                 return (int)e;
         }
     }

@@ -5,8 +5,9 @@
 // Volumes are [B][nz][ny][nx]; projections [B][V][n_rows][C], the view layout
 // the reference's FDK filter walks (FDK/GPURecon_GPU.cu:211).  Voxel centres
 // are x = xmin + dx(i+1/2), y likewise, z = zmin + dz(k+1/2) with
-// zmin = -dz*nz/2 (FDK/FBP.cc:86); the source orbits at z = 0
-// (FDK/GPURecon_GPU.cu:226).
+// zmin = -dz*nz/2 (FDK/FBP.cc:86); the source of view v is at height
+// view_z[v] (0 when the plan has no per-view heights, the reference's
+// FDK/GPURecon_GPU.cu:226).
 #include <cfloat>
 #include <climits>
 
@@ -57,7 +58,8 @@ __device__ __forceinline__ void split_pos(float y, int &i, float &f) {
 template <int ZC, int DEG>
 __global__ void __launch_bounds__(kThreads)
     cone_bp_kernel(const float *__restrict__ proj, float *__restrict__ vol,
-                   const float2 *__restrict__ view_cs, ConeArgs a, int batch) {
+                   const float2 *__restrict__ view_cs, const float *__restrict__ view_z,
+                   ConeArgs a, int batch) {
     const int ix = blockIdx.x * 32 + threadIdx.x;
     const int iy = blockIdx.y * 8 + threadIdx.y;
     const int zgroups = (a.nz + ZC - 1) / ZC;
@@ -90,7 +92,8 @@ __global__ void __launch_bounds__(kThreads)
             const float *pv = pb + (size_t)v * pview;
             // row + 1/2 of slice k0 + kk: rr0 + kk * drr
             const float slope = a.row_scale * rU;
-            const float rr0 = fmaf(z0, slope, a.row_off);
+            const float zs = view_z ? __ldg(view_z + v) : 0.0f;
+            const float rr0 = fmaf(z0 - zs, slope, a.row_off);
             const float drr = a.dz * slope;
 #pragma unroll
             for (int kk = 0; kk < ZC; ++kk) {
@@ -127,7 +130,8 @@ constexpr int kRB = 16;
 template <int DEG>
 __global__ void __launch_bounds__(kThreads)
     cone_bp_transpose_kernel(const float *__restrict__ vol, float *__restrict__ proj,
-                             const float2 *__restrict__ view_cs, ConeArgs a, int batch) {
+                             const float2 *__restrict__ view_cs, const float *__restrict__ view_z,
+                             ConeArgs a, int batch) {
     extern __shared__ float rows_acc[];  // [kRB][C]
     const int rblocks = (a.n_rows + kRB - 1) / kRB;
     const int v = blockIdx.x;
@@ -137,6 +141,7 @@ __global__ void __launch_bounds__(kThreads)
     for (int k = threadIdx.x; k < kRB * a.C; k += kThreads) rows_acc[k] = 0.0f;
     __syncthreads();
     const float2 cs = __ldg(view_cs + v);
+    const float zfirst = a.zmin + 0.5f * a.dz - (view_z ? __ldg(view_z + v) : 0.0f);
     const float *vb = vol + (size_t)b * a.nz * a.ny * a.nx;
     const float rmax = (float)a.n_rows;
     const size_t plane = (size_t)a.nx * a.ny;
@@ -157,7 +162,7 @@ __global__ void __launch_bounds__(kThreads)
         const int i0 = max(ic - 1, 0), i1 = min(ic, a.C - 1);
         const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
         const float slope = a.row_scale * rU;
-        const float rr_first = fmaf(a.zmin + 0.5f * a.dz, slope, a.row_off);  // slice 0
+        const float rr_first = fmaf(zfirst, slope, a.row_off);  // slice 0
         const float drr = a.dz * slope;
         // slices whose row coordinate (clamped) touches rows [R0-1, R0+nr]:
         // rr in (R0 - 0.5, R0 + nr + 0.5], widened by one slice each way
@@ -200,7 +205,8 @@ __global__ void __launch_bounds__(kThreads)
 // volume when most rays run along x) and, per lane, handles RB detector rows
 // at once.  Detector row r sits at height h_r = det_bottom + (r+1/2) drow on
 // the cylinder of radius D about the source; at in-plane distance s the ray
-// is at height z = h_r s / D, so its z cell coordinate is linear in the
+// is at height z = z_s + h_r s / D (z_s the view's source height), so its z
+// cell coordinate is linear in the
 // sample index.  Inside an in-plane cell the bilinear weights are quadratic
 // and the z fraction linear in the sample index, so each (cell, row) sum is
 // exact in closed form from sum j^m, m <= 3 (split where the z cell changes).
@@ -217,7 +223,7 @@ __global__ void __launch_bounds__(kThreads)
     cone_fp_kernel(const float *__restrict__ vol, const float *__restrict__ vol_t,
                    float *__restrict__ proj, const float4 *__restrict__ ray,
                    const int *__restrict__ nsamp, const float2 *__restrict__ chan_s,
-                   ConeFpArgs a, int batch) {
+                   const float *__restrict__ view_z, ConeFpArgs a, int batch) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
@@ -244,11 +250,12 @@ __global__ void __launch_bounds__(kThreads)
     // in-plane distance from the source of sample k: s0 - k * chord / n (mm)
     const float2 sd = has_c ? __ldg(chan_s + c) : make_float2(0.f, 0.f);
     const float ds = valid ? -sd.y / (float)n : 0.0f;
+    const float zs = view_z ? __ldg(view_z + v) : 0.0f;
     float w0[RB], dw[RB], acc[RB];
 #pragma unroll
     for (int rr = 0; rr < RB; ++rr) {
         const float h = a.det_bottom + a.drow * ((float)(r0 + rr) + 0.5f);
-        w0[rr] = (h * sd.x / a.D - a.zmin) / a.dz - 0.5f;
+        w0[rr] = (h * sd.x / a.D + zs - a.zmin) / a.dz - 0.5f;
         dw[rr] = h * ds / (a.D * a.dz);
         acc[rr] = 0.0f;
     }
@@ -433,11 +440,11 @@ int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *st
         float *vp = vol + (size_t)b0 * a.nz * a.ny * a.nx;
         cudaStream_t s = (cudaStream_t)stream;
         if (a.atan_deg == 4)
-            cone_bp_kernel<ZC, 4><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, a, nb);
+            cone_bp_kernel<ZC, 4><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
         else if (a.atan_deg == 8)
-            cone_bp_kernel<ZC, 8><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, a, nb);
+            cone_bp_kernel<ZC, 8><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
         else
-            cone_bp_kernel<ZC, 0><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, a, nb);
+            cone_bp_kernel<ZC, 0><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();
@@ -459,7 +466,7 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
         const int nb = batch - b0 < per ? batch - b0 : per;
         kern<<<dim3(a.V, rblocks * nb), kThreads, smem, (cudaStream_t)stream>>>(
             vol + (size_t)b0 * a.nz * a.ny * a.nx, proj + (size_t)b0 * a.V * a.n_rows * a.C, vcs,
-            a, nb);
+            p->d_view_z, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();
@@ -503,7 +510,7 @@ int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *wo
         cone_fp_kernel<RB><<<dim3(blocks, rgroups * nb), kThreads, 0, s>>>(
             vol + (size_t)b0 * nz * nx * ny, vol_t + (size_t)b0 * nz * nx * ny,
             proj + (size_t)b0 * a.V * a.n_rows * a.C, reinterpret_cast<const float4 *>(p->d_ray),
-            p->d_nsamp, reinterpret_cast<const float2 *>(p->d_chan_s), a, nb);
+            p->d_nsamp, reinterpret_cast<const float2 *>(p->d_chan_s), p->d_view_z, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();

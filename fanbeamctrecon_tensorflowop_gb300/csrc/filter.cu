@@ -56,25 +56,33 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// Elementwise pre-weights over [batch][V][rows][C]: wv[v][c] (short scan)
+// and wr[r][c] (cosine), either may be NULL.
 __global__ void __launch_bounds__(256)
-    parker_kernel(const float *__restrict__ in, float *__restrict__ out,
-                  const float *__restrict__ w, long long total, int C, int rows, int V) {
+    preweight_kernel(const float *__restrict__ in, float *__restrict__ out,
+                     const float *__restrict__ wv, const float *__restrict__ wr, long long total,
+                     int C, int rows, int V) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
         const int i = (int)(e % C);
         const long long vr = e / C;
+        const int r = (int)(vr % rows);
         const int v = (int)((vr / rows) % V);
-        out[e] = in[e] * __ldg(w + (size_t)v * C + i);
+        float w = 1.0f;
+        if (wv) w = __ldg(wv + (size_t)v * C + i);
+        if (wr) w *= __ldg(wr + (size_t)r * C + i);
+        out[e] = in[e] * w;
     }
 }
 
 }  // namespace
 
-int apply_parker(const ct_plan *p, const float *in, float *out, int batch, void *stream) {
+int apply_preweight(const ct_plan *p, const float *in, float *out, int batch, void *stream) {
     const long long total = (long long)batch * p->g.n_views * p->n_rows * p->g.n_cols;
     const long long blocks = (total + 255) / 256;
-    parker_kernel<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, (cudaStream_t)stream>>>(
-        in, out, p->d_parker, total, p->g.n_cols, p->n_rows, p->g.n_views);
+    preweight_kernel<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0,
+                       (cudaStream_t)stream>>>(in, out, p->d_parker, p->d_cosw, total,
+                                               p->g.n_cols, p->n_rows, p->g.n_views);
     ct_count_launch();
     return (int)cudaGetLastError();
 }

@@ -272,6 +272,25 @@ void ct_build_channel_table(const ct_fan_geom *g, ct_host_tables *t) {
     }
 }
 
+// Feldkamp cosine pre-weights (L. A. Feldkamp, L. C. Davis, J. W. Kress,
+// JOSA A 1(6), 1984) per (row, channel) of an equiangular, cylindrical
+// detector: cos(gamma_i), times the cosine of the row's cone angle,
+// D / sqrt(D^2 + h_r^2) with h_r = det_bottom + (r + 1/2) drow, for cone
+// plans; gamma_i = left + (i + 1/2 - shift) dcol as the backprojector maps it.
+void ct_build_cosine(const ct_fan_geom *g, int n_rows, bool cone, ct_host_tables *t) {
+    const int C = g->n_cols;
+    const double D = g->sdd;
+    t->cosw.assign((size_t)n_rows * C, 0.0f);
+    for (int r = 0; r < n_rows; ++r) {
+        const double h = (double)g->det_bottom + (r + 0.5) * (double)g->drow;
+        const double kappa = cone ? D / std::sqrt(D * D + h * h) : 1.0;
+        for (int i = 0; i < C; ++i) {
+            const double gam = (double)g->left + (i + 0.5 - (double)g->shift) * (double)g->dcol;
+            t->cosw[(size_t)r * C + i] = static_cast<float>(std::cos(gam) * kappa);
+        }
+    }
+}
+
 // Parker's short-scan weights (D. L. Parker, Med. Phys. 9(2), 1982) for the
 // ray of view v and channel i: with beta = angle[v] - angle[0] and the
 // channel's fan angle gamma = left + (i + 1/2 - shift) dcol (the angle the

@@ -29,6 +29,8 @@ struct ct_host_tables {
     // sample, and the FOV chord length (mm) (cone-beam projector heights).
     std::vector<float> chan_s;       // [2*C]
     std::vector<float> parker;       // [V*C] short-scan weights (x2), when requested
+    std::vector<float> cosw;         // [n_rows*C] Feldkamp cosine weights, when requested
+    std::vector<float> view_z;       // [V] source heights (mm), when given
     int32_t max_nsamp = 0;
     double total_samples = 0;        // sum of nsamp over all rays
 };
@@ -41,6 +43,7 @@ void ct_build_ray_table(const ct_fan_geom *g, const float *angles, ct_host_table
 void ct_build_filter_taps(const ct_fan_geom *g, int window, ct_host_tables *t);
 void ct_build_channel_table(const ct_fan_geom *g, ct_host_tables *t);
 void ct_build_parker(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
+void ct_build_cosine(const ct_fan_geom *g, int n_rows, bool cone, ct_host_tables *t);
 // Largest |t/U| = tan(gamma) over the FOV disc: rfov / sqrt(R^2 - rfov^2).
 double ct_max_tan_gamma(const ct_fan_geom *g);
 // Fits atan(z) = z * sum_k coef[k] (z^2)^k on |z| <= zmax (interpolation at
@@ -70,6 +73,8 @@ struct ct_plan {
     float *d_tc_hi, *d_tc_lo;        // tensor-core filter: TF32 split of the Toeplitz taps
     int *d_err;                      // raised by kernels whose bounded waits gave up
     float *d_parker;                 // [V*C] short-scan weights, or NULL (full scan)
+    float *d_cosw;                   // [n_rows*C] cosine pre-weights, or NULL
+    float *d_view_z;                 // [V] source heights (mm), or NULL (orbit at z = 0)
 };
 
 // Kernel launchers (defined in the .cu files).  Each returns the launch error.
@@ -89,8 +94,12 @@ int tc_padded(int C);
 bool ramp_tc_supported(int C);
 void build_tc_taps(const float *taps, int C, std::vector<float> &hi, std::vector<float> &lo);
 int ramp_filter_tc(const ct_plan *p, const float *in, float *out, int rows, void *stream);
-// out = in * parker weights (per view and channel; rows and slices broadcast)
-int apply_parker(const ct_plan *p, const float *in, float *out, int batch, void *stream);
+// Whether FBP / FDK weight the projections before filtering (short scan or
+// cosine pre-weighting).
+inline bool has_preweight(const ct_plan *p) { return p->d_parker || p->d_cosw; }
+// out = in * parker[v][c] * cosw[r][c] (each factor when present), over
+// [batch][V][n_rows][C]
+int apply_preweight(const ct_plan *p, const float *in, float *out, int batch, void *stream);
 int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream);
 int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream);
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work, void *stream);

@@ -77,9 +77,9 @@ extern "C" ct_status ct_fbp_fan_static_scratch(const ct_plan *plan, const float 
         return CT_ERR_WORKSPACE;
     }
     if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
-    if (plan->d_parker) {
-        ct_set_last_error("ct_fbp_fan_static_scratch: short-scan plans need a second scratch "
-                          "sinogram; use ct_fbp_fan");
+    if (ctk::has_preweight(plan)) {
+        ct_set_last_error("ct_fbp_fan_static_scratch: short-scan and cosine-weighted plans "
+                          "need a second scratch sinogram; use ct_fbp_fan");
         return CT_ERR_UNSUPPORTED;
     }
     if (plan->device < 0 || plan->device >= kMaxDevices) return CT_ERR_UNSUPPORTED;

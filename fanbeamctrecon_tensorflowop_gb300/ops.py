@@ -32,13 +32,15 @@ class FanPlan:
     nz = 1
 
     def __init__(self, param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK,
-                 filter_algo: int = _lib.FILTER_AUTO, short_scan: bool = False):
+                 filter_algo: int = _lib.FILTER_AUTO, short_scan: bool = False,
+                 cosine_weight: bool = False):
         self._lib = _lib.load()
         self.param16 = np.ascontiguousarray(np.asarray(param16, dtype=np.float32)).copy()
         self.angles = np.ascontiguousarray(np.asarray(angles, dtype=np.float32)).copy()
         self.geom = decode(self.param16)
         self.window = int(window)
         self.short_scan = bool(short_scan)
+        self.cosine_weight = bool(cosine_weight)
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device)
@@ -48,6 +50,7 @@ class FanPlan:
         opts.filter_window = int(window)
         opts.filter_algo = int(filter_algo)
         opts.short_scan = int(self.short_scan)
+        opts.cosine_weight = int(self.cosine_weight)
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             st = self._create(opts, handle)
@@ -198,18 +201,27 @@ class ConePlan(FanPlan):
     """A cone-beam geometry: the fan geometry of ``param16`` (parameter[13..15]
     = detector bottom, row height, slice thickness) with ``n_rows`` detector
     rows and ``nz`` slices.  Volumes are float32 [B, nz, ny, nx], projections
-    float32 [B, n_views, n_rows, n_cols]."""
+    float32 [B, n_views, n_rows, n_cols].  ``source_z`` (mm, one per view)
+    puts the source of each view at that height: a z-offset orbit or a helix;
+    ``cosine_weight`` adds Feldkamp's cos(gamma) cos(cone angle) pre-weight."""
 
     def __init__(self, param16, angles, n_rows: int, nz: int, device=None,
-                 window: int = _lib.WINDOW_RAMLAK, short_scan: bool = False):
+                 window: int = _lib.WINDOW_RAMLAK, short_scan: bool = False,
+                 cosine_weight: bool = False, source_z=None):
         self.n_rows = int(n_rows)
         self.nz = int(nz)
-        super().__init__(param16, angles, device=device, window=window, short_scan=short_scan)
+        self.source_z = (None if source_z is None else
+                         np.ascontiguousarray(np.asarray(source_z, dtype=np.float32)).copy())
+        super().__init__(param16, angles, device=device, window=window, short_scan=short_scan,
+                         cosine_weight=cosine_weight)
 
     def _create(self, opts, handle) -> int:
-        return self._lib.ct_plan_create_cone(
-            ctypes.byref(self.geom), self.n_rows, self.nz,
-            self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+        fptr = ctypes.POINTER(ctypes.c_float)
+        if self.source_z is not None and self.source_z.shape != self.angles.shape:
+            raise ValueError("source_z needs one height per view")
+        zs = None if self.source_z is None else self.source_z.ctypes.data_as(fptr)
+        return self._lib.ct_plan_create_cone_ex(
+            ctypes.byref(self.geom), self.n_rows, self.nz, self.angles.ctypes.data_as(fptr), zs,
             int(self.angles.shape[0]), ctypes.byref(opts), ctypes.byref(handle))
 
     @property

@@ -111,7 +111,14 @@ typedef struct ct_plan_opts {
      * full-scan redundancy factor.  config.py:24 names ParkWeighting but no
      * reference op reads it.  0: full scan (the reference). */
     int32_t short_scan;
-    int32_t reserved[5];    /* must be zero      */
+    /* 1: Feldkamp cosine pre-weighting (Feldkamp, Davis & Kress 1984): FBP,
+     * FDK and their adjoints weight channel i, row r by cos(gamma_i) (fan
+     * plans) or cos(gamma_i) * sdd / sqrt(sdd^2 + h_r^2) (cone plans), with
+     * gamma_i = left + (i + 1/2 - shift) dcol and h_r the row height.  The
+     * reference has none (FBP/transform.cu:61-89 weights by 1/L^2 only).
+     * 0: no pre-weighting (the reference). */
+    int32_t cosine_weight;
+    int32_t reserved[4];    /* must be zero      */
 } ct_plan_opts;
 
 /* Operators, for ct_workspace_size. */
@@ -252,6 +259,17 @@ ct_status ct_fdk_bp(const ct_plan *plan, const float *d_sino, float *d_img, int 
  * drow > 0, dz > 0 and sdd > sid. */
 ct_status ct_plan_create_cone(const ct_fan_geom *geom, int n_rows, int nz, const float *angles,
                               int n_angles, const ct_plan_opts *opts, ct_plan **out);
+
+/* ct_plan_create_cone with the source at height source_z[v] (mm) in view v:
+ * a z-offset circular orbit (all equal) or a helix (source_z[v] = z0 +
+ * pitch * (angle[v] - angle[0]) / (2 pi)).  The reference's view record has
+ * these fields (ViewInfo.fSourceZ / fDeltaZ, FDK/GPURecon_GPU.h:27-33) but
+ * always passes 0 (FDK/GPURecon_GPU.cu:226).  Every cone operator then uses
+ * row = ((z - source_z[v]) * D / U - det_bottom) / drow and rays from the
+ * source at that height.  source_z == NULL is ct_plan_create_cone. */
+ct_status ct_plan_create_cone_ex(const ct_fan_geom *geom, int n_rows, int nz,
+                                 const float *angles, const float *source_z, int n_angles,
+                                 const ct_plan_opts *opts, ct_plan **out);
 
 /* The reference's CB_EA backprojection (FDK/GPURecon_GPU.cu:15-50) over all
  * views, unfiltered: per voxel in the FOV disc and view, the bilinear

@@ -90,7 +90,11 @@ def _l():
         lib.orc_parker_weight.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
         lib.orc_parker_weight.restype = ctypes.c_double
         lib.orc_parker_weights.argtypes = [g, fp_, dp]
+        lib.orc_cosine_weights.argtypes = [g, ctypes.c_int, ctypes.c_int, dp]
         ci = ctypes.c_int
+        lib.orc_cone_bp_zs.argtypes = [g, ci, ci, fp_, fp_, dp, dp, ci]
+        lib.orc_cone_bp_transpose_zs.argtypes = [g, ci, ci, fp_, fp_, dp, dp, ci]
+        lib.orc_cone_fp_zs.argtypes = [g, ci, ci, fp_, fp_, dp, dp, ci]
         lib.orc_cone_bp.argtypes = [g, ci, ci, fp_, dp, dp, ci]
         lib.orc_cone_bp_transpose.argtypes = [g, ci, ci, fp_, dp, dp, ci]
         lib.orc_fdk_cone.argtypes = [g, ci, ci, fp_, ci, dp, dp, ci]
@@ -220,34 +224,46 @@ def parker_weights(g, angles) -> np.ndarray:
     return w
 
 
-def _weighted(g, angles, y, short_scan):
-    """Scales each (view, channel) of y [B, V, (rows,) C] by the Parker table."""
-    if not short_scan:
-        return y
-    w = parker_weights(g, angles)
-    if y.ndim == 4:
-        w = w[:, None, :]
-    return y * w
+def cosine_weights(g, n_rows: int = 1, cone: bool = False) -> np.ndarray:
+    """Feldkamp cosine pre-weights [n_rows, n_cols]."""
+    w = np.zeros((n_rows, g.n_cols), np.float64)
+    _l().orc_cosine_weights(ctypes.byref(g), n_rows, 1 if cone else 0, _dptr(w))
+    return w
 
 
-def fbp_fan(g, angles, sino, window: int = RAMLAK, short_scan: bool = False) -> np.ndarray:
-    y = np.ascontiguousarray(_weighted(g, angles, _batch_sino(g, sino), short_scan))
+def _weighted(g, angles, y, short_scan, cosine=False, n_rows=1, cone=False):
+    """Scales y [B, V, (rows,) C] by the Parker table [V, C] and the cosine
+    table [rows, C], each when requested."""
+    if short_scan:
+        w = parker_weights(g, angles)
+        y = y * (w[:, None, :] if y.ndim == 4 else w)
+    if cosine:
+        w = cosine_weights(g, n_rows, cone)
+        y = y * (w if y.ndim == 4 else w[0])
+    return y
+
+
+def fbp_fan(g, angles, sino, window: int = RAMLAK, short_scan: bool = False,
+            cosine: bool = False) -> np.ndarray:
+    y = np.ascontiguousarray(_weighted(g, angles, _batch_sino(g, sino), short_scan, cosine))
     out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
     _l().orc_fbp_fan(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(y), _dptr(out),
                      y.shape[0])
     return out
 
 
-def fbp_fan_adjoint(g, angles, img, window: int = RAMLAK, short_scan: bool = False) -> np.ndarray:
+def fbp_fan_adjoint(g, angles, img, window: int = RAMLAK, short_scan: bool = False,
+                    cosine: bool = False) -> np.ndarray:
     x = _batch_img(g, img)
     out = np.zeros((x.shape[0], g.n_views, g.n_cols), np.float64)
     _l().orc_fbp_fan_adjoint(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(x),
                              _dptr(out), x.shape[0])
-    return _weighted(g, angles, out, short_scan)
+    return _weighted(g, angles, out, short_scan, cosine)
 
 
-def fdk_bp(g, angles, sino, window: int = RAMLAK, short_scan: bool = False) -> np.ndarray:
-    y = np.ascontiguousarray(_weighted(g, angles, _batch_sino(g, sino), short_scan))
+def fdk_bp(g, angles, sino, window: int = RAMLAK, short_scan: bool = False,
+           cosine: bool = False) -> np.ndarray:
+    y = np.ascontiguousarray(_weighted(g, angles, _batch_sino(g, sino), short_scan, cosine))
     out = np.zeros((y.shape[0], g.ny, g.nx), np.float64)
     _l().orc_fdk_bp(ctypes.byref(g), _fptr(_angles(g, angles)), window, _dptr(y), _dptr(out),
                     y.shape[0])
@@ -274,43 +290,63 @@ def _batch_proj(g, n_rows, proj):
     return y
 
 
-def cone_fp(g, n_rows, nz, angles, vol) -> np.ndarray:
+def _zs(g, source_z):
+    if source_z is None:
+        return None
+    z = np.ascontiguousarray(np.asarray(source_z, np.float32))
+    if z.shape != (g.n_views,):
+        raise ValueError(f"source_z must be [{g.n_views}]")
+    return z
+
+
+def cone_fp(g, n_rows, nz, angles, vol, source_z=None) -> np.ndarray:
     x = _batch_vol(g, nz, vol)
     out = np.zeros((x.shape[0], g.n_views, n_rows, g.n_cols), np.float64)
-    _l().orc_cone_fp(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(x),
-                     _dptr(out), x.shape[0])
+    zs = _zs(g, source_z)
+    if zs is None:
+        _l().orc_cone_fp(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(x),
+                         _dptr(out), x.shape[0])
+    else:
+        _l().orc_cone_fp_zs(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _fptr(zs),
+                            _dptr(x), _dptr(out), x.shape[0])
     return out
 
 
-def cone_bp(g, n_rows, nz, angles, proj) -> np.ndarray:
+def cone_bp(g, n_rows, nz, angles, proj, source_z=None) -> np.ndarray:
     y = _batch_proj(g, n_rows, proj)
     out = np.zeros((y.shape[0], nz, g.ny, g.nx), np.float64)
-    _l().orc_cone_bp(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(y),
-                     _dptr(out), y.shape[0])
+    zs = _zs(g, source_z)
+    if zs is None:
+        _l().orc_cone_bp(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(y),
+                         _dptr(out), y.shape[0])
+    else:
+        _l().orc_cone_bp_zs(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _fptr(zs),
+                            _dptr(y), _dptr(out), y.shape[0])
     return out
 
 
-def cone_bp_transpose(g, n_rows, nz, angles, vol) -> np.ndarray:
+def cone_bp_transpose(g, n_rows, nz, angles, vol, source_z=None) -> np.ndarray:
     x = _batch_vol(g, nz, vol)
     out = np.zeros((x.shape[0], g.n_views, n_rows, g.n_cols), np.float64)
-    _l().orc_cone_bp_transpose(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), _dptr(x),
-                               _dptr(out), x.shape[0])
+    zs = _zs(g, source_z)
+    if zs is None:
+        _l().orc_cone_bp_transpose(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)),
+                                   _dptr(x), _dptr(out), x.shape[0])
+    else:
+        _l().orc_cone_bp_transpose_zs(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)),
+                                      _fptr(zs), _dptr(x), _dptr(out), x.shape[0])
     return out
 
 
-def fdk_cone(g, n_rows, nz, angles, proj, window: int = RAMLAK,
-             short_scan: bool = False) -> np.ndarray:
-    y = np.ascontiguousarray(_weighted(g, angles, _batch_proj(g, n_rows, proj), short_scan))
-    out = np.zeros((y.shape[0], nz, g.ny, g.nx), np.float64)
-    _l().orc_fdk_cone(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), window, _dptr(y),
-                      _dptr(out), y.shape[0])
-    return out
+def fdk_cone(g, n_rows, nz, angles, proj, window: int = RAMLAK, short_scan: bool = False,
+             cosine: bool = False, source_z=None) -> np.ndarray:
+    """FDK: pre-weights (each when requested), the ramp filter of every
+    (view, row), then the CB_EA backprojection."""
+    y = _weighted(g, angles, _batch_proj(g, n_rows, proj), short_scan, cosine, n_rows, True)
+    return cone_bp(g, n_rows, nz, angles, ramp_filter(g, y, window), source_z)
 
 
-def fdk_cone_adjoint(g, n_rows, nz, angles, vol, window: int = RAMLAK,
-                     short_scan: bool = False) -> np.ndarray:
-    x = _batch_vol(g, nz, vol)
-    out = np.zeros((x.shape[0], g.n_views, n_rows, g.n_cols), np.float64)
-    _l().orc_fdk_cone_adjoint(ctypes.byref(g), n_rows, nz, _fptr(_angles(g, angles)), window,
-                              _dptr(x), _dptr(out), x.shape[0])
-    return _weighted(g, angles, out, short_scan)
+def fdk_cone_adjoint(g, n_rows, nz, angles, vol, window: int = RAMLAK, short_scan: bool = False,
+                     cosine: bool = False, source_z=None) -> np.ndarray:
+    t = ramp_filter(g, cone_bp_transpose(g, n_rows, nz, angles, vol, source_z), window)
+    return _weighted(g, angles, t, short_scan, cosine, n_rows, True)

@@ -504,7 +504,8 @@ void orc_fdk_bp(const orc_geom *g, const float *angles, int window, const double
  * (0 < col < C), row = (z * D / U - det_bottom) / drow, bilinear clamped
  * sample of the [n_rows][C] view at (col, row), weight 1/(U^2+t^2). */
 static void cone_bp_impl(const orc_geom *g, int n_rows, int nz, const float *angles,
-                         const double *proj, double *vol, int batch, int transpose) {
+                         const float *zs, const double *proj, double *vol, int batch,
+                         int transpose) {
     const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
     const double r2 = (double)g->rfov * (double)g->rfov;
     const float zmin = -0.5f * g->dz * (float)nz;
@@ -529,8 +530,9 @@ static void cone_bp_impl(const orc_geom *g, int n_rows, int nz, const float *ang
                         if (!bp_col(g, x, y, c, s, &i0, &i1, &f, &U, &t)) continue;
                         const double wgt = 1.0 / (U * U + t * t);
                         const double *pv = pb + (size_t)v * pview;
+                        const double z_src = zs ? (double)zs[v] : 0.0;
                         for (int k = 0; k < nz; ++k) {
-                            const double zk = (double)zmin + (double)g->dz * (k + 0.5);
+                            const double zk = (double)zmin + (double)g->dz * (k + 0.5) - z_src;
                             const double row =
                                 (zk * (double)g->sdd / U - (double)g->det_bottom) / (double)g->drow;
                             const double rb = row - 0.5, rf = floor(rb);
@@ -562,9 +564,10 @@ static void cone_bp_impl(const orc_geom *g, int n_rows, int nz, const float *ang
                         if (!(x * x + y * y <= r2)) continue;
                         if (!bp_col(g, x, y, c, s, &i0, &i1, &f, &U, &t)) continue;
                         const double wgt = 1.0 / (U * U + t * t);
+                        const double z_src = zs ? (double)zs[v] : 0.0;
                         for (int k = 0; k < nz; ++k) {
                             const double val = vb[((size_t)k * ny + j) * nx + i] * wgt;
-                            const double zk = (double)zmin + (double)g->dz * (k + 0.5);
+                            const double zk = (double)zmin + (double)g->dz * (k + 0.5) - z_src;
                             const double row =
                                 (zk * (double)g->sdd / U - (double)g->det_bottom) / (double)g->drow;
                             const double rb = row - 0.5, rf = floor(rb);
@@ -587,12 +590,24 @@ static void cone_bp_impl(const orc_geom *g, int n_rows, int nz, const float *ang
 
 void orc_cone_bp(const orc_geom *g, int n_rows, int nz, const float *angles, const double *proj,
                  double *vol, int batch) {
-    cone_bp_impl(g, n_rows, nz, angles, proj, vol, batch, 0);
+    cone_bp_impl(g, n_rows, nz, angles, NULL, proj, vol, batch, 0);
 }
 
 void orc_cone_bp_transpose(const orc_geom *g, int n_rows, int nz, const float *angles,
                            const double *vol, double *proj, int batch) {
-    cone_bp_impl(g, n_rows, nz, angles, proj, (double *)vol, batch, 1);
+    cone_bp_impl(g, n_rows, nz, angles, NULL, proj, (double *)vol, batch, 1);
+}
+
+/* The same with the source of view v at height zs[v] (mm): the row of a voxel
+ * at z is ((z - zs[v]) * D / U - det_bottom) / drow. */
+void orc_cone_bp_zs(const orc_geom *g, int n_rows, int nz, const float *angles, const float *zs,
+                    const double *proj, double *vol, int batch) {
+    cone_bp_impl(g, n_rows, nz, angles, zs, proj, vol, batch, 0);
+}
+
+void orc_cone_bp_transpose_zs(const orc_geom *g, int n_rows, int nz, const float *angles,
+                              const float *zs, const double *vol, double *proj, int batch) {
+    cone_bp_impl(g, n_rows, nz, angles, zs, proj, (double *)vol, batch, 1);
 }
 
 /* FDK of the reference (BP_One_Rot_3D_GPU, FDK/GPURecon_GPU.cu:163-268) with
@@ -628,8 +643,8 @@ void orc_fdk_cone_adjoint(const orc_geom *g, int n_rows, int nz, const float *an
  * trilinear, clamp-to-edge volume sample (texel centres at +1/2 in x, y, z),
  * and the sum is weighted by 0.125*dx*sqrt(1 + (h_r/D)^2), the 3-D length of
  * one in-plane step. */
-void orc_cone_fp(const orc_geom *g, int n_rows, int nz, const float *angles, const double *vol,
-                 double *proj, int batch) {
+static void cone_fp_impl(const orc_geom *g, int n_rows, int nz, const float *angles,
+                         const float *zs, const double *vol, double *proj, int batch) {
     const int V = g->n_views, C = g->n_cols, nx = g->nx, ny = g->ny;
     const size_t R = (size_t)V * C;
     double *ray = (double *)malloc(sizeof(double) * 4 * R);
@@ -663,7 +678,7 @@ void orc_cone_fp(const orc_geom *g, int n_rows, int nz, const float *angles, con
                 double acc = 0.0;
                 for (int k = 0; k < n; ++k) {
                     const tap4 t = bilinear_taps(nx, ny, q[0] + k * q[2], q[1] + k * q[3]);
-                    const double z = hr * (s0 + k * ds) / D;
+                    const double z = (zs ? (double)zs[v] : 0.0) + hr * (s0 + k * ds) / D;
                     const double wz = (z - (double)zmin) / (double)g->dz - 0.5;
                     const double fz0 = floor(wz);
                     const double az = frac_w(wz - fz0);
@@ -684,4 +699,33 @@ void orc_cone_fp(const orc_geom *g, int n_rows, int nz, const float *angles, con
     }
     free(ray);
     free(ns);
+}
+
+void orc_cone_fp(const orc_geom *g, int n_rows, int nz, const float *angles, const double *vol,
+                 double *proj, int batch) {
+    cone_fp_impl(g, n_rows, nz, angles, NULL, vol, proj, batch);
+}
+
+/* Cone FP with the source of view v at height zs[v]: the ray's height at
+ * in-plane distance s is zs[v] + h_r * s / D. */
+void orc_cone_fp_zs(const orc_geom *g, int n_rows, int nz, const float *angles, const float *zs,
+                    const double *vol, double *proj, int batch) {
+    cone_fp_impl(g, n_rows, nz, angles, zs, vol, proj, batch);
+}
+
+/* Feldkamp cosine pre-weights [n_rows][C]: cos(gam_i), times
+ * D / sqrt(D^2 + h_r^2) when cone != 0 (the cone angle of row r of the
+ * cylindrical detector), gam_i = left + (i + 1/2 - shift) dcol. */
+void orc_cosine_weights(const orc_geom *g, int n_rows, int cone, double *w) {
+    const int C = g->n_cols;
+    const double D = g->sdd;
+    for (int r = 0; r < n_rows; ++r) {
+        const double h = (double)g->det_bottom + (r + 0.5) * (double)g->drow;
+        for (int i = 0; i < C; ++i) {
+            const double gam = (double)g->left + (i + 0.5 - (double)g->shift) * (double)g->dcol;
+            /* cos(gam) * cos(kappa) with tan(kappa) = h / D */
+            const double ck = cone ? 1.0 / sqrt(1.0 + (h / D) * (h / D)) : 1.0;
+            w[(size_t)r * C + i] = cos(gam) * ck;
+        }
+    }
 }
