@@ -411,34 +411,47 @@ def main() -> None:
                                                                     dtype=torch.bfloat16)))
             rays += pl.geom.n_views * pl.geom.n_cols
         ubs = [UnevenBatch(fp_items), UnevenBatch(fbp_items), UnevenBatch(adj_items)]
+
+        def graph_ms():
+            for ub in ubs:
+                ub.run()
+            torch.cuda.synchronize(dev)
+            graph = torch.cuda.CUDAGraph()
+            cap = torch.cuda.Stream(dev)
+            cap.wait_stream(stream)
+            with torch.cuda.stream(cap):
+                with torch.cuda.graph(graph, stream=cap):
+                    for ub in ubs:
+                        ub.run()
+            stream.wait_stream(cap)
+            for _ in range(args.warmup):
+                graph.replay()
+            barrier()
+            n_rep = max(3, args.steps // 3)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(n_rep):
+                graph.replay()
+            e1.record(stream)
+            barrier()
+            return max_over_ranks(e0.elapsed_time(e1)) / n_rep
+
         for ub in ubs:
-            ub.run()
-        torch.cuda.synchronize(dev)
-        graph = torch.cuda.CUDAGraph()
-        cap = torch.cuda.Stream(dev)
-        cap.wait_stream(stream)
-        with torch.cuda.stream(cap):
-            with torch.cuda.graph(graph, stream=cap):
-                for ub in ubs:
-                    ub.run()
-        stream.wait_stream(cap)
-        for _ in range(args.warmup):
-            graph.replay()
-        barrier()
-        n_rep = max(3, args.steps // 3)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(n_rep):
-            graph.replay()
-        e1.record(stream)
-        barrier()
-        g_ms = max_over_ranks(e0.elapsed_time(e1)) / n_rep
+            ub.set_config(None)
+        g_default = graph_ms()
+        # the autotuner picks both persistent launches' shapes per batch
+        t_tune = time.perf_counter()
+        tuned = [ub.tune(reps=2) for ub in ubs]
+        t_tune = time.perf_counter() - t_tune
+        g_ms = graph_ms()
         uneven = {"workload": "48 slices cycling 256^2/492x512, 384^2/720x736, 512^2/984x888, "
                               "BF16 storage: FP + FBP + FBP adjoint of every slice, 3 "
                               "ct_batch_run calls in one CUDA graph",
-                  "graph_replay_ms": g_ms, "slice_ops_per_replay": 144,
-                  "fp_rays_per_replay": rays}
-        del ubs, graph, fp_items, fbp_items, adj_items
+                  "graph_replay_ms": g_ms, "graph_replay_ms_default_shapes": g_default,
+                  "tuned_shapes": {"fp": tuned[0], "fbp": tuned[1], "fbp_adjoint": tuned[2]},
+                  "tune_seconds": t_tune,
+                  "slice_ops_per_replay": 144, "fp_rays_per_replay": rays}
+        del ubs, fp_items, fbp_items, adj_items
 
     # ---- e2e through the reference-named entry point with host buffers ---------------
     host_imgs = [imgs[k].cpu().numpy() for k in range(2)]

@@ -69,6 +69,17 @@ DTYPE_BF16 = 1
 BATCH_MAX_ITEMS = 64
 
 
+class CtBatchConfig(ctypes.Structure):
+    """Mirror of ct_batch_config."""
+
+    _fields_ = [("fp_blocks_per_sm", ctypes.c_int32), ("fp_dynamic", ctypes.c_int32),
+                ("bp_blocks_per_sm", ctypes.c_int32), ("bp_dynamic", ctypes.c_int32),
+                ("bp_tile_rows", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class CtPlanOpts(ctypes.Structure):
     _fields_ = [("filter_window", ctypes.c_int32), ("filter_algo", ctypes.c_int32),
                 ("short_scan", ctypes.c_int32), ("cosine_weight", ctypes.c_int32),
@@ -112,6 +123,11 @@ SIGNATURES = {
     "ct_fp_cone": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ct_batch_workspace_size": (_i, [_P(CtBatchItem), _i, _P(_sz)]),
     "ct_batch_run": (_i, [_P(CtBatchItem), _i, _vp, _sz, _vp]),
+    "ct_batch_tune": (_i, [_P(CtBatchItem), _i, _vp, _sz, ctypes.c_int32, _vp,
+                           _P(CtBatchConfig)]),
+    "ct_batch_get_config": (_i, [_P(CtBatchItem), _i, _P(CtBatchConfig),
+                                 _P(ctypes.c_int32)]),
+    "ct_batch_set_config": (_i, [_P(CtBatchItem), _i, _P(CtBatchConfig)]),
     "ct_fbp_fan_static_scratch": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_plain_fp_fan_adjoint": (_i, [_vp, _vp, _vp, _i, _vp]),

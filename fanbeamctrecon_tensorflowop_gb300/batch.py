@@ -3,6 +3,7 @@ types in one ``ct_batch_run`` call (one persistent FP launch, one persistent
 BP launch), optionally captured once in a CUDA graph and replayed.
 
     ub = UnevenBatch([(plan_a, "fp", img_a, sino_a), (plan_b, "fbp", sino_b, img_b), ...])
+    ub.tune()                # optional: pick the launch shapes for this batch
     ub.run()                 # eager
     ub.capture(); ub.replay()  # CUDA graph
 
@@ -66,6 +67,36 @@ class UnevenBatch:
                                         self.work.numel(),
                                         torch.cuda.current_stream(self.device).cuda_stream)
         _lib.check(st, "ct_batch_run")
+
+    def tune(self, reps: int = 3) -> dict:
+        """Times every candidate launch shape of the two persistent launches on
+        this batch (outputs are overwritten) and keeps the fastest for this
+        batch shape; later run() / capture() calls use it.  Returns it."""
+        cfg = _lib.CtBatchConfig()
+        with torch.cuda.device(self.device):
+            st = self._lib.ct_batch_tune(self._arr, len(self.items), self.work.data_ptr(),
+                                         self.work.numel(), int(reps),
+                                         torch.cuda.current_stream(self.device).cuda_stream,
+                                         ctypes.byref(cfg))
+        _lib.check(st, "ct_batch_tune")
+        return cfg.as_dict()
+
+    @property
+    def config(self) -> tuple[dict, bool]:
+        """(launch shape run() uses, whether it was tuned or set)."""
+        cfg, tuned = _lib.CtBatchConfig(), ctypes.c_int32()
+        _lib.check(self._lib.ct_batch_get_config(self._arr, len(self.items), ctypes.byref(cfg),
+                                                 ctypes.byref(tuned)), "ct_batch_get_config")
+        return cfg.as_dict(), bool(tuned.value)
+
+    def set_config(self, cfg: dict | None) -> None:
+        """Records a launch shape for this batch shape (None forgets it)."""
+        if cfg is None:
+            st = self._lib.ct_batch_set_config(self._arr, len(self.items), None)
+        else:
+            c = _lib.CtBatchConfig(**cfg)
+            st = self._lib.ct_batch_set_config(self._arr, len(self.items), ctypes.byref(c))
+        _lib.check(st, "ct_batch_set_config")
 
     def capture(self) -> "torch.cuda.CUDAGraph":
         """Records one run() into a CUDA graph (after an eager warm-up run)."""

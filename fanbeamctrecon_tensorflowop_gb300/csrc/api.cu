@@ -544,7 +544,55 @@ ct_status ct_batch_run(const ct_batch_item *items, int n, void *d_work, size_t w
     Workspace w;
     st = acquire(w, d_work, work_bytes, need, stream);
     if (st != CT_OK) return st;
-    return launch_status(ctk::batch_run(items, n, w.ptr, stream), "ct_batch_run");
+    const ct_batch_config cfg = ctk::batch_lookup(items, n, nullptr);
+    return launch_status(ctk::batch_run(items, n, w.ptr, stream, cfg, nullptr), "ct_batch_run");
+}
+
+ct_status ct_batch_tune(const ct_batch_item *items, int n, void *d_work, size_t work_bytes,
+                        int32_t reps, ct_stream stream, ct_batch_config *out) {
+    size_t need = 0;
+    ct_status st = ctk::batch_workspace(items, n, &need);
+    if (st != CT_OK || n == 0) return st;
+    DeviceScope ds(items[0].plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamIsCapturing");
+    if (cap != cudaStreamCaptureStatusNone) {
+        ct_set_last_error("ct_batch_tune: the stream is being captured; tune before capture");
+        return CT_ERR_INVALID_ARGUMENT;
+    }
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, need, stream);
+    if (st != CT_OK) return st;
+    ct_batch_config best{};
+    st = launch_status(ctk::batch_tune(items, n, w.ptr, stream, reps > 0 ? reps : 3, &best),
+                       "ct_batch_tune");
+    if (st != CT_OK) return st;
+    ctk::batch_store(items, n, &best);
+    if (out) *out = best;
+    return CT_OK;
+}
+
+ct_status ct_batch_get_config(const ct_batch_item *items, int n, ct_batch_config *out,
+                              int32_t *tuned) {
+    if (!out) return CT_ERR_NULL_POINTER;
+    size_t need = 0;
+    ct_status st = ctk::batch_workspace(items, n, &need);
+    if (st != CT_OK) return st;
+    bool t = false;
+    *out = ctk::batch_lookup(items, n, &t);
+    if (tuned) *tuned = t ? 1 : 0;
+    return CT_OK;
+}
+
+ct_status ct_batch_set_config(const ct_batch_item *items, int n, const ct_batch_config *config) {
+    size_t need = 0;
+    ct_status st = ctk::batch_workspace(items, n, &need);
+    if (st != CT_OK) return st;
+    if (config && (st = ctk::batch_check_config(*config)) != CT_OK) return st;
+    ctk::batch_store(items, n, config);
+    return CT_OK;
 }
 
 ct_status ct_plain_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int batch,

@@ -13,8 +13,18 @@
 //   5. one launch narrows the FBP-adjoint results that are stored as BF16.
 // Item descriptors travel as __grid_constant__ kernel parameters, so a call
 // needs no host-to-device copy and can be captured in a CUDA graph.
+//
+// The two persistent launches take their shape from a ct_batch_config: grid
+// size (blocks per SM), fixed-stride or dynamic (atomic counter, largest item
+// first) distribution of units, and the BP tile height.  batch_tune times the
+// candidates on the caller's batch and keeps the fastest per batch shape.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
 #include <vector>
 
 #include "bp_body.cuh"
@@ -99,9 +109,26 @@ __global__ void __launch_bounds__(256) quads_batch_kernel(const __grid_constant_
     }
 }
 
-__global__ void __launch_bounds__(256) fp_batch_kernel(const __grid_constant__ FpBatch P) {
+// Next unit of a warp: fixed stride, or the next value of the launch's
+// atomic counter (units are ordered largest item first in that mode).
+template <bool DYN>
+__device__ __forceinline__ int next_warp_unit(int *ctr, int prev, int first, int step) {
+    if constexpr (DYN) {
+        int u = 0;
+        if ((threadIdx.x & 31) == 0) u = atomicAdd(ctr, 1);
+        return __shfl_sync(0xffffffffu, u, 0);
+    } else {
+        return prev < 0 ? first : prev + step;
+    }
+}
+
+template <bool DYN>
+__global__ void __launch_bounds__(256)
+    fp_batch_kernel(const __grid_constant__ FpBatch P, int *ctr) {
     const int step = gridDim.x * 8;
-    for (int gw = blockIdx.x * 8 + (threadIdx.x >> 5); gw < P.total; gw += step) {
+    const int first = blockIdx.x * 8 + (threadIdx.x >> 5);
+    for (int gw = next_warp_unit<DYN>(ctr, -1, first, step); gw < P.total;
+         gw = next_warp_unit<DYN>(ctr, gw, first, step)) {
         const FpItem &it = P.it[find_item(P.it, P.n, gw)];  // warp-uniform
         const int unit = gw - it.unit0;
         if (it.out_bf16)
@@ -114,31 +141,47 @@ __global__ void __launch_bounds__(256) fp_batch_kernel(const __grid_constant__ F
     }
 }
 
-template <bool W, int DEG>
+template <bool W, int DEG, int ROWS>
 __device__ __forceinline__ void bp_item_tile(const BpItem &it, int tx, int ty) {
     if (it.out_bf16)
-        bp_tile<W, 1, DEG, __nv_bfloat16>(it.sino, 0, static_cast<__nv_bfloat16 *>(it.img), 0,
-                                          it.view_cs, it.a, 1, tx, ty);
+        bp_tile<W, 1, DEG, __nv_bfloat16, ROWS>(it.sino, 0, static_cast<__nv_bfloat16 *>(it.img),
+                                                0, it.view_cs, it.a, 1, tx, ty);
     else
-        bp_tile<W, 1, DEG, float>(it.sino, 0, static_cast<float *>(it.img), 0, it.view_cs, it.a,
-                                  1, tx, ty);
+        bp_tile<W, 1, DEG, float, ROWS>(it.sino, 0, static_cast<float *>(it.img), 0, it.view_cs,
+                                        it.a, 1, tx, ty);
 }
 
-__global__ void __launch_bounds__(256) bp_batch_kernel(const __grid_constant__ BpBatch P) {
-    for (int u = blockIdx.x; u < P.total; u += gridDim.x) {  // block-uniform
+// Next tile of a block (block-uniform): fixed stride or the atomic counter.
+template <bool DYN>
+__device__ __forceinline__ int next_block_unit(int *ctr, int prev) {
+    if constexpr (DYN) {
+        __shared__ int s_unit;
+        __syncthreads();  // every thread has read the previous value
+        if (threadIdx.x == 0 && threadIdx.y == 0) s_unit = atomicAdd(ctr, 1);
+        __syncthreads();
+        return s_unit;
+    } else {
+        return prev < 0 ? (int)blockIdx.x : prev + (int)gridDim.x;
+    }
+}
+
+template <bool DYN, int ROWS>
+__global__ void __launch_bounds__(256)
+    bp_batch_kernel(const __grid_constant__ BpBatch P, int *ctr) {
+    for (int u = next_block_unit<DYN>(ctr, -1); u < P.total; u = next_block_unit<DYN>(ctr, u)) {
         const BpItem &it = P.it[find_item(P.it, P.n, u)];
         const int local = u - it.unit0;
         const int ty = local / it.tiles_x, tx = local - ty * it.tiles_x;
         if (it.use_atanf) {
             if (it.weighted)
-                bp_item_tile<true, 0>(it, tx, ty);
+                bp_item_tile<true, 0, ROWS>(it, tx, ty);
             else
-                bp_item_tile<false, 0>(it, tx, ty);
+                bp_item_tile<false, 0, ROWS>(it, tx, ty);
         } else {
             if (it.weighted)
-                bp_item_tile<true, 8>(it, tx, ty);
+                bp_item_tile<true, 8, ROWS>(it, tx, ty);
             else
-                bp_item_tile<false, 8>(it, tx, ty);
+                bp_item_tile<false, 8, ROWS>(it, tx, ty);
         }
     }
 }
@@ -181,10 +224,12 @@ BpArgs bp_args(const ct_plan *p) {
 size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 
 struct Layout {
-    // byte offsets into the workspace, per item (SIZE_MAX = unused)
+    // byte offsets into the workspace, per item (SIZE_MAX = unused); the
+    // first 256 bytes hold the dynamic-schedule counters
     std::vector<size_t> quads, in32, filt, out32, wtd;
     size_t total = 0;
 };
+constexpr size_t kCounterBytes = 256;
 
 Layout plan_layout(const ct_batch_item *items, int n) {
     Layout L;
@@ -193,7 +238,7 @@ Layout plan_layout(const ct_batch_item *items, int n) {
     L.filt.assign(n, SIZE_MAX);
     L.out32.assign(n, SIZE_MAX);
     L.wtd.assign(n, SIZE_MAX);
-    size_t off = 0;
+    size_t off = kCounterBytes;
     auto take = [&](size_t bytes) {
         const size_t o = off;
         off += align256(bytes);
@@ -268,19 +313,42 @@ ct_status batch_workspace(const ct_batch_item *items, int n, size_t *bytes) {
 }
 
 // Enqueues the whole batch on `stream`; returns a CUDA error code.
-int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
+// Items in launch order: as given, or (dynamic schedule) by decreasing work
+// so that the largest items are taken first.
+std::vector<int> order_by_work(const ct_batch_item *items, int n, bool largest_first, bool fp) {
+    std::vector<int> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    if (largest_first) {
+        auto work = [&](int i) {
+            const ct_plan *p = items[i].plan;
+            // FP: rays x path length; BP: pixels x views
+            return fp ? (double)p->g.n_views * p->g.n_cols * p->g.nx
+                      : (double)p->g.nx * p->g.ny * p->g.n_views;
+        };
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return work(a) > work(b); });
+    }
+    return idx;
+}
+
+int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
+              const ct_batch_config &cfg, void **ev) {
     cudaStream_t s = (cudaStream_t)stream;
     const Layout L = plan_layout(items, n);
     uint8_t *ws = static_cast<uint8_t *>(work);
     auto at = [&](size_t off) { return static_cast<void *>(ws + off); };
     const int sms = sm_count();
-    cudaError_t e;
+    cudaError_t e = cudaSuccess;
+
+    int *ctr = static_cast<int *>(work);  // [0]: FP units, [1]: BP tiles
+    const bool dyn_any = cfg.fp_dynamic || cfg.bp_dynamic;
+    if (dyn_any && (e = cudaMemsetAsync(ctr, 0, 2 * sizeof(int), s)) != cudaSuccess) return (int)e;
+    cudaEvent_t *evs = reinterpret_cast<cudaEvent_t *>(ev);
 
     // 1-2: forward projections
     {
         QuadBatch QB{};
         FpBatch FB{};
-        for (int i = 0; i < n; ++i) {
+        for (int i : order_by_work(items, n, cfg.fp_dynamic != 0, true)) {
             if (items[i].op != CT_OP_FP) continue;
             const ct_plan *p = items[i].plan;
             const int Q = p->g.nx + 1;
@@ -312,8 +380,13 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
         if (QB.n > 0) {
             quads_batch_kernel<<<QB.total < sms * 16 ? QB.total : sms * 16, dim3(32, 8), 0, s>>>(
                 QB);
-            fp_batch_kernel<<<(FB.total + 7) / 8 < sms * 3 ? (FB.total + 7) / 8 : sms * 3, 256, 0,
-                              s>>>(FB);
+            const int cap = sms * cfg.fp_blocks_per_sm, want = (FB.total + 7) / 8;
+            if (evs) cudaEventRecord(evs[0], s);
+            if (cfg.fp_dynamic)
+                fp_batch_kernel<true><<<want < cap ? want : cap, 256, 0, s>>>(FB, ctr);
+            else
+                fp_batch_kernel<false><<<want < cap ? want : cap, 256, 0, s>>>(FB, ctr);
+            if (evs) cudaEventRecord(evs[1], s);
             ct_count_launch(2);
             if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
         }
@@ -371,7 +444,8 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
     // 4: backprojections of BP and FBP items
     {
         BpBatch BB{};
-        for (int i = 0; i < n; ++i) {
+        const int tile_h = cfg.bp_tile_rows;
+        for (int i : order_by_work(items, n, cfg.bp_dynamic != 0, false)) {
             if (items[i].op != CT_OP_BP && items[i].op != CT_OP_FBP) continue;
             const ct_plan *p = items[i].plan;
             const bool bf = items[i].dtype == CT_DTYPE_BF16;
@@ -389,10 +463,24 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
             b.out_bf16 = bf;
             b.weighted = items[i].op == CT_OP_FBP;
             b.use_atanf = p->atan_deg == 0;
-            BB.total += b.tiles_x * ((p->g.ny + kBpTile - 1) / kBpTile);
+            BB.total += b.tiles_x * ((p->g.ny + tile_h - 1) / tile_h);
         }
         if (BB.n > 0) {
-            bp_batch_kernel<<<BB.total < sms * 4 ? BB.total : sms * 4, dim3(32, 8), 0, s>>>(BB);
+            const int cap = sms * cfg.bp_blocks_per_sm;
+            const dim3 grid(BB.total < cap ? BB.total : cap), block(32, 8);
+            if (evs) cudaEventRecord(evs[2], s);
+            if (cfg.bp_dynamic) {
+                if (tile_h == 16)
+                    bp_batch_kernel<true, 2><<<grid, block, 0, s>>>(BB, ctr + 1);
+                else
+                    bp_batch_kernel<true, 4><<<grid, block, 0, s>>>(BB, ctr + 1);
+            } else {
+                if (tile_h == 16)
+                    bp_batch_kernel<false, 2><<<grid, block, 0, s>>>(BB, ctr + 1);
+                else
+                    bp_batch_kernel<false, 4><<<grid, block, 0, s>>>(BB, ctr + 1);
+            }
+            if (evs) cudaEventRecord(evs[3], s);
             ct_count_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
         }
@@ -415,6 +503,136 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream) {
         }
     }
     return (int)cudaGetLastError();
+}
+
+ct_batch_config batch_default_config() {
+    ct_batch_config c{};
+    c.fp_blocks_per_sm = 3;
+    c.fp_dynamic = 0;
+    c.bp_blocks_per_sm = 4;
+    c.bp_dynamic = 0;
+    c.bp_tile_rows = 32;
+    return c;
+}
+
+ct_status batch_check_config(const ct_batch_config &c) {
+    if (c.fp_blocks_per_sm < 1 || c.fp_blocks_per_sm > 16 || c.bp_blocks_per_sm < 1 ||
+        c.bp_blocks_per_sm > 16 || (c.fp_dynamic != 0 && c.fp_dynamic != 1) ||
+        (c.bp_dynamic != 0 && c.bp_dynamic != 1) ||
+        (c.bp_tile_rows != 16 && c.bp_tile_rows != 32))
+        return CT_ERR_INVALID_ARGUMENT;
+    for (int r : c.reserved)
+        if (r != 0) return CT_ERR_INVALID_ARGUMENT;
+    return CT_OK;
+}
+
+namespace {
+
+std::mutex g_cfg_mu;
+std::map<std::string, ct_batch_config> g_cfg;
+
+// Batch shape: device and, per item, operator, storage type and sizes.
+std::string batch_key(const ct_batch_item *items, int n) {
+    std::string k = std::to_string(n > 0 ? items[0].plan->device : -1);
+    for (int i = 0; i < n; ++i) {
+        const ct_plan *p = items[i].plan;
+        k += '|' + std::to_string(items[i].op) + ',' + std::to_string(items[i].dtype) + ',' +
+             std::to_string(p->g.nx) + ',' + std::to_string(p->g.ny) + ',' +
+             std::to_string(p->g.n_views) + ',' + std::to_string(p->g.n_cols);
+    }
+    return k;
+}
+
+}  // namespace
+
+ct_batch_config batch_lookup(const ct_batch_item *items, int n, bool *tuned) {
+    std::lock_guard<std::mutex> lock(g_cfg_mu);
+    auto it = g_cfg.find(batch_key(items, n));
+    if (tuned) *tuned = it != g_cfg.end();
+    return it != g_cfg.end() ? it->second : batch_default_config();
+}
+
+void batch_store(const ct_batch_item *items, int n, const ct_batch_config *c) {
+    std::lock_guard<std::mutex> lock(g_cfg_mu);
+    if (c)
+        g_cfg[batch_key(items, n)] = *c;
+    else
+        g_cfg.erase(batch_key(items, n));
+}
+
+// Candidates: FP {1,2,3,4,6,8} blocks/SM x {stride, dynamic}; BP {2,3,4,6,8,
+// 12} blocks/SM x {stride, dynamic} x {32, 16}-row tiles.  Run k pairs FP
+// candidate k mod 12 with BP candidate k mod 24, so 24 runs per repetition
+// time every candidate of both launches; each candidate keeps its fastest
+// repetition.
+int batch_tune(const ct_batch_item *items, int n, void *work, void *stream, int reps,
+               ct_batch_config *best) {
+    static const int kFpBlocks[] = {1, 2, 3, 4, 6, 8};
+    static const int kBpBlocks[] = {2, 3, 4, 6, 8, 12};
+    std::vector<ct_batch_config> fpc, bpc;
+    for (int dyn = 0; dyn < 2; ++dyn)
+        for (int b : kFpBlocks) {
+            ct_batch_config c = batch_default_config();
+            c.fp_blocks_per_sm = b;
+            c.fp_dynamic = dyn;
+            fpc.push_back(c);
+        }
+    for (int rows : {32, 16})
+        for (int dyn = 0; dyn < 2; ++dyn)
+            for (int b : kBpBlocks) {
+                ct_batch_config c = batch_default_config();
+                c.bp_blocks_per_sm = b;
+                c.bp_dynamic = dyn;
+                c.bp_tile_rows = rows;
+                bpc.push_back(c);
+            }
+    const int runs = (int)std::max(fpc.size(), bpc.size());
+    std::vector<float> fpt(fpc.size(), 1e30f), bpt(bpc.size(), 1e30f);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t ev[4] = {};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
+    bool has_fp = false, has_bp = false;
+    for (int i = 0; i < n; ++i) {
+        has_fp |= items[i].op == CT_OP_FP;
+        has_bp |= items[i].op == CT_OP_BP || items[i].op == CT_OP_FBP;
+    }
+    // one untimed run first (module load, first-touch of the workspace)
+    if (e == cudaSuccess)
+        e = (cudaError_t)batch_run(items, n, work, stream, batch_default_config(), nullptr);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+        for (int k = 0; k < runs && e == cudaSuccess; ++k) {
+            ct_batch_config c = fpc[k % fpc.size()];
+            const ct_batch_config &b = bpc[k % bpc.size()];
+            c.bp_blocks_per_sm = b.bp_blocks_per_sm;
+            c.bp_dynamic = b.bp_dynamic;
+            c.bp_tile_rows = b.bp_tile_rows;
+            e = (cudaError_t)batch_run(items, n, work, stream, c, reinterpret_cast<void **>(ev));
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            float ms = 0.0f;
+            if (e == cudaSuccess && has_fp && cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess)
+                fpt[k % fpc.size()] = std::min(fpt[k % fpc.size()], ms);
+            if (e == cudaSuccess && has_bp && cudaEventElapsedTime(&ms, ev[2], ev[3]) == cudaSuccess)
+                bpt[k % bpc.size()] = std::min(bpt[k % bpc.size()], ms);
+        }
+    }
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    if (e != cudaSuccess) return (int)e;
+    const size_t bf = std::min_element(fpt.begin(), fpt.end()) - fpt.begin();
+    const size_t bb = std::min_element(bpt.begin(), bpt.end()) - bpt.begin();
+    ct_batch_config c = batch_default_config();
+    if (has_fp) {
+        c.fp_blocks_per_sm = fpc[bf].fp_blocks_per_sm;
+        c.fp_dynamic = fpc[bf].fp_dynamic;
+    }
+    if (has_bp) {
+        c.bp_blocks_per_sm = bpc[bb].bp_blocks_per_sm;
+        c.bp_dynamic = bpc[bb].bp_dynamic;
+        c.bp_tile_rows = bpc[bb].bp_tile_rows;
+    }
+    *best = c;
+    return (int)cudaSuccess;
 }
 
 }  // namespace ctk

@@ -41,34 +41,35 @@ __device__ __forceinline__ void split_pos(float y, int &i, float &f) {
     f = y - (m - 12582912.0f);
 }
 
-// One 32x32 tile (tx, ty) of nsl <= SB slices: sino slice s at
+// One 32 x (8 ROWS) tile (tx, ty) of nsl <= SB slices: sino slice s at
 // sino + s * sstride ([V][C]), image slice s at img + s * istride ([ny][nx]).
-// Block of 32 x 8 threads, four pixels per thread; block-uniform call.
-template <bool WEIGHTED, int SB, int DEG, typename OutT>
+// Block of 32 x 8 threads, ROWS pixels per thread (32 x 32 tiles by default);
+// block-uniform call.
+template <bool WEIGHTED, int SB, int DEG, typename OutT, int ROWS = kBpRowsPerThr>
 __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t sstride,
                                         OutT *__restrict__ img, size_t istride,
                                         const float2 *__restrict__ view_cs, const BpArgs &a,
                                         int nsl, int tx, int ty) {
     const int ix = tx * kBpTile + threadIdx.x;
-    const int iy0 = ty * kBpTile + threadIdx.y;
-    float py[kBpRowsPerThr];
-    bool in[kBpRowsPerThr];
+    const int iy0 = ty * (8 * ROWS) + threadIdx.y;
+    float py[ROWS];
+    bool in[ROWS];
     const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
     const float px = (float)xd;
     bool any = false;
 #pragma unroll
-    for (int k = 0; k < kBpRowsPerThr; ++k) {
+    for (int k = 0; k < ROWS; ++k) {
         const int iy = iy0 + 8 * k;
         const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
         py[k] = (float)yd;
         in[k] = ix < a.nx && iy < a.ny && (xd * xd + yd * yd <= a.fov_r2);
         any |= in[k];
     }
-    float acc[SB][kBpRowsPerThr];
+    float acc[SB][ROWS];
 #pragma unroll
     for (int s = 0; s < SB; ++s)
 #pragma unroll
-        for (int k = 0; k < kBpRowsPerThr; ++k) acc[s][k] = 0.0f;
+        for (int k = 0; k < ROWS; ++k) acc[s][k] = 0.0f;
     if (__syncthreads_or(any)) {
         const float *sb[SB];
 #pragma unroll
@@ -77,7 +78,7 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
             const float2 cs = __ldg(view_cs + v);
             const size_t ro = (size_t)v * a.C;
 #pragma unroll
-            for (int k = 0; k < kBpRowsPerThr; ++k) {
+            for (int k = 0; k < ROWS; ++k) {
                 const float U = fmaf(px, cs.x, fmaf(py[k], cs.y, a.R));
                 const float t = fmaf(py[k], cs.x, -px * cs.y);
                 const float rU = __fdividef(1.0f, U);
@@ -105,7 +106,7 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
         if (s >= nsl) break;
         OutT *ib = img + (size_t)s * istride;
 #pragma unroll
-        for (int k = 0; k < kBpRowsPerThr; ++k) {
+        for (int k = 0; k < ROWS; ++k) {
             const int iy = iy0 + 8 * k;
             if (ix < a.nx && iy < a.ny) store_val(ib + (size_t)iy * a.nx + ix, acc[s][k]);
         }

@@ -105,7 +105,20 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work, void *stream);
 size_t cone_fp_work_bytes(const ct_plan *p, int batch);
 ct_status batch_workspace(const ct_batch_item *items, int n, size_t *bytes);
-int batch_run(const ct_batch_item *items, int n, void *work, void *stream);
+// Enqueues the batch with launch shape `cfg`; when `ev` (four cudaEvent_t)
+// is not NULL, records ev[0], ev[1] around the persistent FP launch and
+// ev[2], ev[3] around the persistent BP launch.
+int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
+              const ct_batch_config &cfg, void **ev);
+ct_batch_config batch_default_config();
+ct_status batch_check_config(const ct_batch_config &c);
+// The configuration kept for this batch shape (default when none); *tuned
+// tells which.
+ct_batch_config batch_lookup(const ct_batch_item *items, int n, bool *tuned);
+void batch_store(const ct_batch_item *items, int n, const ct_batch_config *c);
+// Times the candidate launch shapes (see ct_batch_tune); returns a CUDA error.
+int batch_tune(const ct_batch_item *items, int n, void *work, void *stream, int reps,
+               ct_batch_config *best);
 int plain_fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *stream);
 int plain_fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
 int plain_bp_fan(const ct_plan *p, const float *sino, float *img, int batch, void *stream);

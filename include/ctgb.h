@@ -335,6 +335,38 @@ ct_status ct_batch_workspace_size(const ct_batch_item *items, int n, size_t *byt
 ct_status ct_batch_run(const ct_batch_item *items, int n, void *d_work, size_t work_bytes,
                        ct_stream stream);
 
+/* Launch shapes of ct_batch_run's two persistent launches.  The library
+ * keeps one configuration per batch shape (the ops, storage types and sizes
+ * of the items, in order); ct_batch_run uses it, or the default below for a
+ * shape that was never tuned or set. */
+typedef struct ct_batch_config {
+    int32_t fp_blocks_per_sm; /* FP launch: 256-thread blocks per SM, 1..16 (default 3)  */
+    int32_t fp_dynamic;       /* 1: warps take (item, view, 32 channels) units from an
+                                 atomic counter, largest item first; 0: fixed stride */
+    int32_t bp_blocks_per_sm; /* BP launch: 256-thread blocks per SM, 1..16 (default 4)  */
+    int32_t bp_dynamic;       /* as fp_dynamic, for BP tiles                               */
+    int32_t bp_tile_rows;     /* BP tile height in pixels: 32 or 16 (tiles are 32 wide)  */
+    int32_t reserved[3];      /* zero                                                     */
+} ct_batch_config;
+
+/* Project-written autotuner: runs the batch (its outputs are overwritten)
+ * with every candidate launch shape, `reps` times each (reps <= 0: 3), timing
+ * the FP and BP launches separately with CUDA events, and keeps the fastest
+ * FP shape and the fastest BP shape for this batch shape.  Synchronises
+ * `stream`; must not run during stream capture.  The chosen configuration is
+ * written to *out when out != NULL. */
+ct_status ct_batch_tune(const ct_batch_item *items, int n, void *d_work, size_t work_bytes,
+                        int32_t reps, ct_stream stream, ct_batch_config *out);
+
+/* The configuration ct_batch_run uses for this batch shape; *tuned = 1 if it
+ * was tuned or set, 0 for the default. */
+ct_status ct_batch_get_config(const ct_batch_item *items, int n, ct_batch_config *out,
+                              int32_t *tuned);
+
+/* Records a configuration for this batch shape (e.g. one saved from an
+ * earlier ct_batch_tune); config == NULL forgets it. */
+ct_status ct_batch_set_config(const ct_batch_item *items, int n, const ct_batch_config *config);
+
 /* ---- filtered backprojection that allocates nothing ----------------------- */
 
 /* Capacity, in floats, of the fixed device array ct_fbp_fan_static_scratch

@@ -111,3 +111,57 @@ def test_batch_validation(cuda):
     with pytest.raises(TypeError):
         plan, op, x, y = items[0]
         UnevenBatch([(plan, op, x.to(torch.bfloat16), y)])
+
+
+CONFIGS = [
+    dict(fp_blocks_per_sm=1, fp_dynamic=1, bp_blocks_per_sm=2, bp_dynamic=1, bp_tile_rows=16),
+    dict(fp_blocks_per_sm=8, fp_dynamic=0, bp_blocks_per_sm=12, bp_dynamic=0, bp_tile_rows=16),
+    dict(fp_blocks_per_sm=2, fp_dynamic=1, bp_blocks_per_sm=6, bp_dynamic=1, bp_tile_rows=32),
+]
+
+
+def test_every_launch_shape_gives_the_same_result(cuda):
+    """Each unit's arithmetic is independent of which warp or block takes it, so
+    every launch shape reproduces the default's FP and BP outputs bit for bit."""
+    items, _ = _make(cuda, torch.float32, ops=("fp", "fbp", "bp"), n_items=6)
+    ub = UnevenBatch(items)
+    ub.set_config(None)
+    ub.run()
+    base = [y.clone() for *_, y in items]
+    for cfg in CONFIGS:
+        ub.set_config(cfg)
+        assert ub.config == ({**cfg}, True)
+        for *_, y in items:
+            y.fill_(float("nan"))
+        ub.run()
+        for (plan, op, x, y), want in zip(items, base):
+            assert torch.equal(y, want), (cfg, op)
+    ub.set_config(None)
+    assert ub.config[1] is False
+
+
+def test_tune_then_capture(cuda):
+    items, ref = _make(cuda, torch.bfloat16, n_items=8)
+    ub = UnevenBatch(items)
+    cfg = ub.tune(reps=1)
+    assert ub.config == (cfg, True)
+    assert 1 <= cfg["fp_blocks_per_sm"] <= 8 and 2 <= cfg["bp_blocks_per_sm"] <= 12
+    assert cfg["bp_tile_rows"] in (16, 32)
+    ub.capture()
+    for *_, y in items:
+        y.fill_(float("nan"))
+    ub.replay()
+    for (plan, op, x, y), want in zip(items, ref):
+        assert rel_l2(_np(y), _np(want)) <= 8e-3, op
+    ub.set_config(None)
+
+
+def test_config_validation(cuda):
+    items, _ = _make(cuda, torch.float32, n_items=2)
+    ub = UnevenBatch(items)
+    for bad in (dict(fp_blocks_per_sm=0), dict(bp_tile_rows=24), dict(fp_dynamic=2),
+                dict(bp_blocks_per_sm=17)):
+        cfg = {**ub.config[0], **bad}
+        with pytest.raises(RuntimeError):
+            ub.set_config(cfg)
+    assert ub.config[1] is False
