@@ -91,6 +91,8 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
             return parker * proj_bytes(p, batch);
         case CT_OP_FP:
             return ctk::fp_fan_work_bytes(p, batch);
+        case CT_OP_FP_ADJOINT:
+            return ctk::fp_fan_adjoint_work_bytes(p, batch);
         case CT_OP_FBP:
         case CT_OP_FBP_ADJOINT:
         case CT_OP_FDK_BP:
@@ -104,6 +106,7 @@ void free_plan(ct_plan *p) {
     if (!p) return;
     cudaFree(p->d_view_cs);
     cudaFree(p->d_ray);
+    cudaFree(p->d_ray_inv);
     cudaFree(p->d_nsamp);
     cudaFree(p->d_taps);
     cudaFree(p->d_chan_s);
@@ -243,6 +246,21 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
     p->fp_weight = (float)(CT_FP_STEP * (double)geom->dx);
     p->fov_r2 = geom->rfov * geom->rfov;
     p->atan_deg = ct_fit_atan(1.02 * ct_max_tan_gamma(geom), p->atan_coef);
+    {
+        // cells up to 1.5 pixels outside the FOV disc (the adjoint gather)
+        const double r = (double)geom->rfov + 1.5 * (double)geom->dx, R = geom->sid;
+        p->gather_atan_deg =
+            r < R ? ct_fit_atan(1.02 * r / std::sqrt(R * R - r * r), p->gather_atan_coef) : 0;
+        if (!(r < R))
+            for (float &c : p->gather_atan_coef) c = 0.0f;
+    }
+    std::vector<float> ray_inv(t.ray.size() / 2);
+    for (size_t r = 0; r < ray_inv.size() / 2; ++r)
+        for (int k = 0; k < 2; ++k) {
+            const float st = t.ray[4 * r + 2 + k];
+            // a zero step gets 1e30: the adjoint's support bounds become +-inf-like
+            ray_inv[2 * r + k] = st != 0.0f ? (float)(1.0 / (double)st) : 1e30f;
+        }
     p->n_rows = n_rows;
     p->nz = nz;
     p->total_samples = t.total_samples;
@@ -255,6 +273,7 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
     }
     if ((st = upload(&p->d_view_cs, t.view_cs)) != CT_OK ||
         (st = upload(&p->d_ray, t.ray)) != CT_OK || (st = upload(&p->d_nsamp, t.nsamp)) != CT_OK ||
+        (st = upload(&p->d_ray_inv, ray_inv)) != CT_OK ||
         (st = upload(&p->d_taps, t.taps)) != CT_OK ||
         (st = upload(&p->d_chan_s, t.chan_s)) != CT_OK ||
         (st = upload(&p->d_parker, t.parker)) != CT_OK ||
@@ -355,13 +374,14 @@ ct_status ct_fp_fan(const ct_plan *plan, const float *d_img, float *d_sino, int 
 
 ct_status ct_fp_fan_adjoint(const ct_plan *plan, const float *d_sino, float *d_img, int batch,
                             void *d_work, size_t work_bytes, ct_stream stream) {
-    (void)d_work;
-    (void)work_bytes;
     ct_status st = check_call(plan, d_sino, d_img, batch);
     if (st != CT_OK || batch == 0) return st;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
-    return launch_status(ctk::fp_fan_adjoint(plan, d_sino, d_img, batch, stream),
+    Workspace w;
+    st = acquire(w, d_work, work_bytes, op_workspace(plan, CT_OP_FP_ADJOINT, batch), stream);
+    if (st != CT_OK) return st;
+    return launch_status(ctk::fp_fan_adjoint(plan, d_sino, d_img, batch, w.ptr, stream),
                          "ct_fp_fan_adjoint");
 }
 

@@ -61,12 +61,15 @@ struct ct_plan {
     int n_rows, nz;                  // cone plans; 1 and 1 for fan plans
     int atan_deg;                    // 4 or 8: polynomial atan on the FOV; 0: atanf
     float atan_coef[9];
+    int gather_atan_deg;             // the same fit on the FOV widened by 1.5 pixels
+    float gather_atan_coef[9];
     double total_samples;
     int32_t max_nsamp;
     std::vector<float> h_view_cs;    // host copy of the view table
     // device copies of ct_host_tables (owned)
     float *d_view_cs;                // [2V]
     float *d_ray;                    // [4VC]
+    float *d_ray_inv;                // [2VC] 1/step (1e30 for a zero step), adjoint gather
     int32_t *d_nsamp;                // [VC]
     float *d_taps;                   // [2C-1]
     float *d_chan_s;                 // [2C]
@@ -83,7 +86,11 @@ namespace ctk {
 int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *work,
            void *stream);
 size_t fp_fan_work_bytes(const ct_plan *p, int batch);
-int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *stream);
+// work: fp_fan_adjoint_work_bytes(p, batch) bytes (corner sums of up to 64 slices)
+size_t fp_fan_adjoint_work_bytes(const ct_plan *p, int batch);
+int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *work,
+                   void *stream);
+
 // mode 0: unweighted BP, 1: 1/(U^2+t^2)-weighted (FBP / FDK 2-D)
 int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weighted, void *stream);
 int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch, int weighted,
