@@ -33,6 +33,12 @@ namespace ctk {
 namespace {
 
 constexpr int kGThreads = 256;  // 32 x 8 cells per block
+#ifndef CT_ADJ_MIN_BLOCKS
+#define CT_ADJ_MIN_BLOCKS 2
+#endif
+#ifndef CT_ADJ_MAX_SB
+#define CT_ADJ_MAX_SB 8
+#endif
 
 struct CellArgs {
     int V, C, nx, ny;
@@ -64,8 +70,52 @@ __device__ __forceinline__ float chan_of(float u, float v, float2 cs, const Cell
     return (g - a.left) * a.inv_dcol;
 }
 
+// Two FP32 lanes in one 64-bit register: the f32x2 FMA does both slices of a
+// pair in one instruction (each lane rounds as fmaf does).
+__device__ __forceinline__ unsigned long long pack2(float x, float y) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+    return r;
+}
+__device__ __forceinline__ float2 unpack2(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// [nb][V][C] -> [ceil(nb/SB)][V][C][SB] (missing slices of the last group are
+// zero): one (view, channel) holds its SB slices in SB/4 aligned float4s.
+template <int SB>
+__global__ void __launch_bounds__(256)
+    interleave_kernel(const float *__restrict__ sino, float *__restrict__ out, int nb,
+                      size_t slice) {
+    const size_t groups = (nb + SB - 1) / SB;
+    const size_t total = groups * slice;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t g = e / slice, r = e - g * slice;
+        float v[SB];
+#pragma unroll
+        for (int s = 0; s < SB; ++s) {
+            const size_t b = g * SB + s;
+            v[s] = b < (size_t)nb ? __ldg(sino + b * slice + r) : 0.0f;
+        }
+        float4 *o = reinterpret_cast<float4 *>(out + e * SB);
+#pragma unroll
+        for (int q = 0; q < SB / 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+}
+
+// Thread = one cell; the SB slices of a group come interleaved
+// ([V][C][SB], SB = 4 or 8) and accumulate in f32x2 pairs.
 template <int SB, int DEG>
-__global__ void __launch_bounds__(kGThreads)
+__global__ void __launch_bounds__(kGThreads, CT_ADJ_MIN_BLOCKS)
     fp_adjoint_cells_kernel(const float *__restrict__ sino, float *__restrict__ corners,
                             const float4 *__restrict__ ray, const float2 *__restrict__ ray_inv,
                             const int *__restrict__ nsamp, const float2 *__restrict__ view_cs,
@@ -85,11 +135,13 @@ __global__ void __launch_bounds__(kGThreads)
     const bool inside = ic < NXC && jc < NYC;
     const float dxc = uc - a.fov, dyc = vcn - a.fov;
     const bool act = inside && (ext || dxc * dxc + dyc * dyc <= a.skip_r2);
-    float w00[SB], w10[SB], w01[SB], w11[SB];
+    static_assert(SB == 4 || SB == 8, "slices per group");
+    constexpr int NP = SB / 2;  // f32x2 pairs
+    unsigned long long w00[NP], w10[NP], w01[NP], w11[NP];
 #pragma unroll
-    for (int s = 0; s < SB; ++s) w00[s] = w10[s] = w01[s] = w11[s] = 0.0f;
+    for (int s = 0; s < NP; ++s) w00[s] = w10[s] = w01[s] = w11[s] = 0ull;
     const size_t slice = (size_t)a.V * a.C;
-    const float *sb = sino + (size_t)b0 * slice;
+    const float4 *sb = reinterpret_cast<const float4 *>(sino + (size_t)blockIdx.z * slice * SB);
     if (__syncthreads_or(act) && act) {
         for (int v = 0; v < a.V; ++v) {
             const float2 cs = __ldg(view_cs + v);
@@ -161,15 +213,20 @@ __global__ void __launch_bounds__(kGThreads)
                 const float P = fu * fv * cnt + fmaf(fu, sv, fv * su) * S1 + su * sv * S2;
                 const float F = fmaf(fu, cnt, su * S1), G = fmaf(fv, cnt, sv * S1);
                 const float W11 = P, W10 = F - P, W01 = G - P, W00 = cnt - F - G + P;
+                const unsigned long long p00 = pack2(W00, W00), p10 = pack2(W10, W10);
+                const unsigned long long p01 = pack2(W01, W01), p11 = pack2(W11, W11);
 #pragma unroll
-                for (int s = 0; s < SB; ++s) {
-                    if (s < nsl) {
-                        const float val = __ldg(sb + s * slice + row + c);
-                        w00[s] = fmaf(W00, val, w00[s]);
-                        w10[s] = fmaf(W10, val, w10[s]);
-                        w01[s] = fmaf(W01, val, w01[s]);
-                        w11[s] = fmaf(W11, val, w11[s]);
-                    }
+                for (int q = 0; q < SB / 4; ++q) {
+                    const float4 val = __ldg(sb + (row + c) * (SB / 4) + q);
+                    const unsigned long long lo = pack2(val.x, val.y), hi = pack2(val.z, val.w);
+                    w00[2 * q] = fma2(p00, lo, w00[2 * q]);
+                    w00[2 * q + 1] = fma2(p00, hi, w00[2 * q + 1]);
+                    w10[2 * q] = fma2(p10, lo, w10[2 * q]);
+                    w10[2 * q + 1] = fma2(p10, hi, w10[2 * q + 1]);
+                    w01[2 * q] = fma2(p01, lo, w01[2 * q]);
+                    w01[2 * q + 1] = fma2(p01, hi, w01[2 * q + 1]);
+                    w11[2 * q] = fma2(p11, lo, w11[2 * q]);
+                    w11[2 * q + 1] = fma2(p11, hi, w11[2 * q + 1]);
                 }
             }
         }
@@ -177,13 +234,19 @@ __global__ void __launch_bounds__(kGThreads)
     if (inside) {
         const size_t plane = (size_t)NXC * NYC, o = (size_t)jc * NXC + ic;
 #pragma unroll
-        for (int s = 0; s < SB; ++s) {
-            if (s >= nsl) break;
-            float *cb = corners + (size_t)(b0 + s) * 4 * plane;
-            cb[o] = w00[s];
-            cb[plane + o] = w10[s];
-            cb[2 * plane + o] = w01[s];
-            cb[3 * plane + o] = w11[s];
+        for (int q = 0; q < NP; ++q) {
+            const float2 c00 = unpack2(w00[q]), c10 = unpack2(w10[q]);
+            const float2 c01 = unpack2(w01[q]), c11 = unpack2(w11[q]);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int s = 2 * q + h;
+                if (s >= nsl) break;
+                float *cb = corners + (size_t)(b0 + s) * 4 * plane;
+                cb[o] = h ? c00.y : c00.x;
+                cb[plane + o] = h ? c10.y : c10.x;
+                cb[2 * plane + o] = h ? c01.y : c01.x;
+                cb[3 * plane + o] = h ? c11.y : c11.x;
+            }
         }
     }
 }
@@ -209,8 +272,11 @@ __global__ void __launch_bounds__(256)
 }  // namespace
 
 size_t fp_fan_adjoint_work_bytes(const ct_plan *p, int batch) {
-    const int chunk = batch < 64 ? batch : 64;
-    return sizeof(float) * 4 * (size_t)chunk * (p->g.nx + 1) * (p->g.ny + 1);
+    const size_t chunk = batch < 64 ? batch : 64;
+    // corner sums of a chunk, then the chunk's sinograms in groups of 8
+    return sizeof(float) * chunk * (4 * (size_t)(p->g.nx + 1) * (p->g.ny + 1) +
+                                    (size_t)p->g.n_views * p->g.n_cols) +
+           sizeof(float) * 8 * (size_t)p->g.n_views * p->g.n_cols + 256;
 }
 
 int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *work,
@@ -233,29 +299,37 @@ int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, v
     const float4 *ray = reinterpret_cast<const float4 *>(p->d_ray);
     const float2 *rinv = reinterpret_cast<const float2 *>(p->d_ray_inv);
     cudaStream_t s = (cudaStream_t)stream;
-    float *corners = static_cast<float *>(work);
     const size_t plane = (size_t)a.nx * a.ny, slice = (size_t)a.V * a.C;
+    const int chunk = batch < 64 ? batch : 64;
+    float *corners = static_cast<float *>(work);
+    // interleaved sinograms after the corner sums, 16-byte aligned
+    const size_t coff = ((4 * (size_t)chunk * (a.nx + 1) * (a.ny + 1) * sizeof(float) + 255) / 256) * 256;
+    float *inter = reinterpret_cast<float *>(static_cast<char *>(work) + coff);
     for (int b0 = 0; b0 < batch; b0 += 64) {
         const int nb = batch - b0 < 64 ? batch - b0 : 64;
-        const int SB = nb >= 8 ? 8 : (nb >= 4 ? 4 : 1);
-        dim3 grid((a.nx + 1 + 31) / 32, (a.ny + 1 + 7) / 8, (nb + SB - 1) / SB);
+        const int SB = nb >= 8 ? 8 : 4;
+        const int groups = (nb + SB - 1) / SB;
         const float *sp = sino + b0 * slice;
+        const long long work_items = (long long)groups * slice;
+        const int ib = (int)((work_items + 255) / 256 < 152 * 16 ? (work_items + 255) / 256 : 152 * 16);
+        if (SB == 8)
+            interleave_kernel<8><<<ib, 256, 0, s>>>(sp, inter, nb, slice);
+        else
+            interleave_kernel<4><<<ib, 256, 0, s>>>(sp, inter, nb, slice);
+        dim3 grid((a.nx + 1 + 31) / 32, (a.ny + 1 + 7) / 8, groups);
         auto go = [&](auto kern) {
-            kern<<<grid, dim3(32, 8), 0, s>>>(sp, corners, ray, rinv, p->d_nsamp, vcs, a, nb);
+            kern<<<grid, dim3(32, 8), 0, s>>>(inter, corners, ray, rinv, p->d_nsamp, vcs, a, nb);
         };
         if (SB == 8)
             deg == 8 ? go(fp_adjoint_cells_kernel<8, 8>)
                      : deg == 4 ? go(fp_adjoint_cells_kernel<8, 4>) : go(fp_adjoint_cells_kernel<8, 0>);
-        else if (SB == 4)
+        else
             deg == 8 ? go(fp_adjoint_cells_kernel<4, 8>)
                      : deg == 4 ? go(fp_adjoint_cells_kernel<4, 4>) : go(fp_adjoint_cells_kernel<4, 0>);
-        else
-            deg == 8 ? go(fp_adjoint_cells_kernel<1, 8>)
-                     : deg == 4 ? go(fp_adjoint_cells_kernel<1, 4>) : go(fp_adjoint_cells_kernel<1, 0>);
-        fp_adjoint_combine_kernel<<<dim3((a.nx + 31) / 32, (a.ny + 7) / 8, nb < 64 ? nb : 64),
+        fp_adjoint_combine_kernel<<<dim3((a.nx + 31) / 32, (a.ny + 7) / 8, nb),
                                     dim3(32, 8), 0, s>>>(corners, img + b0 * plane, a.nx, a.ny,
                                                          p->fp_weight, nb);
-        ct_count_launch(2);
+        ct_count_launch(3);
     }
     return (int)cudaGetLastError();
 }
