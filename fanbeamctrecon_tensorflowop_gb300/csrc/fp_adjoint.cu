@@ -13,7 +13,7 @@
 // for each computes the range of samples inside the cell (both neighbours of
 // a cell boundary use the same threshold, so every sample lands in exactly
 // one cell) and the four corner sums in closed form from sum j and sum j^2,
-// times p[v,c] for up to 8 slices.  A second pass adds, per texel, the
+// times p[v,c] for up to 16 slices.  A second pass adds, per texel, the
 // matching corner of its four cells.
 //
 // Candidate rays of a view: the ray through the cell centre has fan angle
@@ -33,12 +33,13 @@ namespace ctk {
 namespace {
 
 constexpr int kGThreads = 256;  // 32 x 8 cells per block
-#ifndef CT_ADJ_MIN_BLOCKS
-#define CT_ADJ_MIN_BLOCKS 2
-#endif
 #ifndef CT_ADJ_MAX_SB
-#define CT_ADJ_MAX_SB 8
+#define CT_ADJ_MAX_SB 16
 #endif
+// Resident blocks per SM the register allocation must allow (measured best on
+// GB300 for 32 clinical slices: 16 slices x 2 blocks 11.4 ms, 8 x 3 15.0 ms,
+// 8 x 2 19.7 ms, 16 x 1 19.1 ms).
+constexpr int adj_min_blocks(int sb) { return sb >= 16 ? 2 : (sb >= 8 ? 3 : 4); }
 
 struct CellArgs {
     int V, C, nx, ny;
@@ -113,9 +114,9 @@ __global__ void __launch_bounds__(256)
 }
 
 // Thread = one cell; the SB slices of a group come interleaved
-// ([V][C][SB], SB = 4 or 8) and accumulate in f32x2 pairs.
+// ([V][C][SB], SB = 4, 8 or 16) and accumulate in f32x2 pairs.
 template <int SB, int DEG>
-__global__ void __launch_bounds__(kGThreads, CT_ADJ_MIN_BLOCKS)
+__global__ void __launch_bounds__(kGThreads, adj_min_blocks(SB))
     fp_adjoint_cells_kernel(const float *__restrict__ sino, float *__restrict__ corners,
                             const float4 *__restrict__ ray, const float2 *__restrict__ ray_inv,
                             const int *__restrict__ nsamp, const float2 *__restrict__ view_cs,
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(kGThreads, CT_ADJ_MIN_BLOCKS)
     const bool inside = ic < NXC && jc < NYC;
     const float dxc = uc - a.fov, dyc = vcn - a.fov;
     const bool act = inside && (ext || dxc * dxc + dyc * dyc <= a.skip_r2);
-    static_assert(SB == 4 || SB == 8, "slices per group");
+    static_assert(SB == 4 || SB == 8 || SB == 16, "slices per group");
     constexpr int NP = SB / 2;  // f32x2 pairs
     unsigned long long w00[NP], w10[NP], w01[NP], w11[NP];
 #pragma unroll
@@ -276,7 +277,7 @@ size_t fp_fan_adjoint_work_bytes(const ct_plan *p, int batch) {
     // corner sums of a chunk, then the chunk's sinograms in groups of 8
     return sizeof(float) * chunk * (4 * (size_t)(p->g.nx + 1) * (p->g.ny + 1) +
                                     (size_t)p->g.n_views * p->g.n_cols) +
-           sizeof(float) * 8 * (size_t)p->g.n_views * p->g.n_cols + 256;
+           sizeof(float) * 16 * (size_t)p->g.n_views * p->g.n_cols + 256;
 }
 
 int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *work,
@@ -307,12 +308,14 @@ int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, v
     float *inter = reinterpret_cast<float *>(static_cast<char *>(work) + coff);
     for (int b0 = 0; b0 < batch; b0 += 64) {
         const int nb = batch - b0 < 64 ? batch - b0 : 64;
-        const int SB = nb >= 8 ? 8 : 4;
+        const int SB = nb >= 16 && CT_ADJ_MAX_SB >= 16 ? 16 : (nb >= 8 ? 8 : 4);
         const int groups = (nb + SB - 1) / SB;
         const float *sp = sino + b0 * slice;
         const long long work_items = (long long)groups * slice;
         const int ib = (int)((work_items + 255) / 256 < 152 * 16 ? (work_items + 255) / 256 : 152 * 16);
-        if (SB == 8)
+        if (SB == 16)
+            interleave_kernel<16><<<ib, 256, 0, s>>>(sp, inter, nb, slice);
+        else if (SB == 8)
             interleave_kernel<8><<<ib, 256, 0, s>>>(sp, inter, nb, slice);
         else
             interleave_kernel<4><<<ib, 256, 0, s>>>(sp, inter, nb, slice);
@@ -320,7 +323,10 @@ int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, v
         auto go = [&](auto kern) {
             kern<<<grid, dim3(32, 8), 0, s>>>(inter, corners, ray, rinv, p->d_nsamp, vcs, a, nb);
         };
-        if (SB == 8)
+        if (CT_ADJ_MAX_SB >= 16 && SB == 16)
+            deg == 8 ? go(fp_adjoint_cells_kernel<16, 8>)
+                     : deg == 4 ? go(fp_adjoint_cells_kernel<16, 4>) : go(fp_adjoint_cells_kernel<16, 0>);
+        else if (SB == 8)
             deg == 8 ? go(fp_adjoint_cells_kernel<8, 8>)
                      : deg == 4 ? go(fp_adjoint_cells_kernel<8, 4>) : go(fp_adjoint_cells_kernel<8, 0>);
         else
