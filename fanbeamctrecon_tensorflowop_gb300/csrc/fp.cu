@@ -20,7 +20,10 @@ namespace {
 constexpr int kFpThreads = 256;
 constexpr int kFpChunk = 64;  // slices per quad-workspace chunk
 #ifndef CT_FP_MIN_BLOCKS
-#define CT_FP_MIN_BLOCKS 1
+#define CT_FP_MIN_BLOCKS 2
+#endif
+#ifndef CT_FP_MAX_SB
+#define CT_FP_MAX_SB 16
 #endif
 
 // Builds both quad layouts of nz slices (grid.z = 2 * slices).
@@ -79,12 +82,20 @@ int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *wor
         ct_count_launch();
         float *out = sino + (size_t)c0 * n_rays;
         int b = 0;
-        if (nb >= 8) {
-            const int n8 = nb / 8 * 8;
-            fp_fan_kernel<8><<<dim3(blocks, n8 / 8), kFpThreads, 0, s>>>(
-                quads, out, ray, p->d_nsamp, V, C, wpv, nx, p->fp_weight, n8, max_iter);
+        if (CT_FP_MAX_SB >= 16 && nb >= 16) {
+            const int n16 = nb / 16 * 16;
+            fp_fan_kernel<16><<<dim3(blocks, n16 / 16), kFpThreads, 0, s>>>(
+                quads, out, ray, p->d_nsamp, V, C, wpv, nx, p->fp_weight, n16, max_iter);
             ct_count_launch();
-            b = n8;
+            b = n16;
+        }
+        if (nb - b >= 8) {
+            const int n8 = (nb - b) / 8 * 8;
+            fp_fan_kernel<8><<<dim3(blocks, n8 / 8), kFpThreads, 0, s>>>(
+                quads + (size_t)b * 2 * Q * Q, out + (size_t)b * n_rays, ray, p->d_nsamp, V, C,
+                wpv, nx, p->fp_weight, n8, max_iter);
+            ct_count_launch();
+            b += n8;
         }
         if (nb - b >= 4) {
             fp_fan_kernel<4><<<dim3(blocks, 1), kFpThreads, 0, s>>>(

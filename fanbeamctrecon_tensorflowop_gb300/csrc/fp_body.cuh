@@ -18,24 +18,47 @@ __device__ __forceinline__ float load_val(const __nv_bfloat16 *p) {
     return __bfloat162float(__ldg(p));
 }
 
+// Two FP32 lanes in one 64-bit register for the f32x2 FMA (each lane rounds
+// as fmaf does).
+__device__ __forceinline__ unsigned long long pack2(float x, float y) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+    return r;
+}
+__device__ __forceinline__ float2 unpack2(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// Per slice the cell's dot product w . taps runs as two f32x2 FMAs into a
+// pair (w00 t.x + w01 t.z, w10 t.y + w11 t.w), summed at the end.
 template <int SB>
 struct Taps {
     const float4 *q;  // this warp's layout of the first slice; slice s adds s * stride
     size_t stride;    // quads between consecutive slices
     int Q;            // quads per row (nx + 1)
-    float acc[SB];
+    unsigned long long acc[SB];
     __device__ __forceinline__ void add(const CellWeights &cw, int cu, int cv) {
         const int qi = min(max(cu + 1, 0), Q - 1), qj = min(max(cv + 1, 0), Q - 1);
         const float4 *p = q + (size_t)qj * Q + qi;
+        const unsigned long long wa = pack2(cw.w00, cw.w10), wb = pack2(cw.w01, cw.w11);
 #pragma unroll
         for (int s = 0; s < SB; ++s) {
             const float4 t = __ldg(p + s * stride);
-            float v = cw.w00 * t.x;
-            v = fmaf(cw.w10, t.y, v);
-            v = fmaf(cw.w01, t.z, v);
-            v = fmaf(cw.w11, t.w, v);
-            acc[s] += v;
+            acc[s] = fma2(wa, pack2(t.x, t.y), acc[s]);
+            acc[s] = fma2(wb, pack2(t.z, t.w), acc[s]);
         }
+    }
+    __device__ __forceinline__ float sum(int s) const {
+        const float2 v = unpack2(acc[s]);
+        return v.x + v.y;
     }
 };
 
@@ -76,7 +99,7 @@ __device__ __forceinline__ void fp_warp(const float4 *__restrict__ quads, size_t
     tp.stride = qstride;
     tp.q = quads + (along_x ? lsz : 0);
 #pragma unroll
-    for (int s = 0; s < SB; ++s) tp.acc[s] = 0.0f;
+    for (int s = 0; s < SB; ++s) tp.acc[s] = 0ull;
     const unsigned pm = __ballot_sync(FULL, valid && seg.sv > 0.0f);
     const int dir = 2 * __popc(pm) >= __popc(vm) ? 1 : -1;
     const bool synced = valid && (dir > 0 ? seg.sv > 0.0f : seg.sv < 0.0f);
@@ -131,7 +154,7 @@ __device__ __forceinline__ void fp_warp(const float4 *__restrict__ quads, size_t
     if (has_c) {
 #pragma unroll
         for (int s = 0; s < SB; ++s)
-            if (s < nsl) store_val(out + (size_t)s * ostride + (size_t)v * C + c, tp.acc[s] * w);
+            if (s < nsl) store_val(out + (size_t)s * ostride + (size_t)v * C + c, tp.sum(s) * w);
     }
 }
 
