@@ -47,6 +47,9 @@ POOL = 4
 WORKLOAD = ("fan-beam FP, batch of 32 seeded ellipse phantoms 512x512 @0.7 mm, "
             "984 views x 888 equiangular channels (1 mm pitch), SID 541 / SDD 949 mm")
 GATHER_BYTES_PER_SAMPLE = 16  # four FP32 bilinear taps per ray sample
+FLOP_PER_SAMPLE = 16          # 2 FMA position, 2 fractions, 3 lerps, 1 add (FMA = 2)
+# FP32 FMA peak, derived: 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz (max SM clock)
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
 
 
 def c1_geometry():
@@ -296,12 +299,22 @@ def main() -> None:
     mean_launch = sum(per_fp) / len(per_fp)
     achieved_gbs = GATHER_BYTES_PER_SAMPLE * samples_per_launch / mean_launch / 1e9
     traffic = profiled_traffic("fp_fan_kernel")
+    fp32_tflops = FLOP_PER_SAMPLE * samples_per_launch / mean_launch / 1e12
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
                 "traffic": traffic, "peak_source": peaks["source"],
                 "kernel": "fp_fan_kernel",
                 "algorithmic": f"{GATHER_BYTES_PER_SAMPLE} B/sample x {samples_per_launch:.4g} "
-                               "samples per launch (effective bilinear gather bytes)"}
+                               "samples per launch (effective bilinear gather bytes)",
+                "timed": "per-step CUDA events (the step is build_quads_kernel + "
+                         "fp_fan_kernel; the quad build is ~3% of it)",
+                "note": "the cell walk sums each cell's ~6 samples in closed form, so per-sample "
+                        "work runs above the per-sample peaks; DRAM is far from the bound",
+                "dram_gbs": (traffic / mean_launch / 1e9) if traffic else None,
+                "fp32": {"achieved_tflops": fp32_tflops, "peak_tflops": FP32_PEAK_TFLOPS,
+                         "frac": fp32_tflops / FP32_PEAK_TFLOPS,
+                         "peak_source": "derived: 152 SMs x 128 x 2 FLOP x 2.07 GHz",
+                         "algorithmic": f"{FLOP_PER_SAMPLE} FLOP/sample"}}
 
     # ---- BP throughput ------------------------------------------------------------
     def bp_step(k):
@@ -329,6 +342,14 @@ def main() -> None:
     n_fa = max(5, args.steps // 3)
     total_fa, _, _ = timed(fwd_adj_step, n_fa, args.warmup)
     fa_ms = 1e3 * total_fa / n_fa
+
+    def adj_step(k):
+        plan.fp_adjoint(sinos[k % POOL], out=grads[k % 2])
+
+    total_adj, per_adj, _ = timed(adj_step, n_fa, args.warmup)
+    adj_ms = 1e3 * total_adj / n_fa
+    adj_gather_gbs = GATHER_BYTES_PER_SAMPLE * samples_per_launch / (
+        sum(per_adj) / len(per_adj)) / 1e9
 
     plain_ms = None
     if not args.no_plain:
@@ -496,6 +517,8 @@ def main() -> None:
                 "bp_gpix_views_per_s": bp_gpv,
                 "fbp_shepp_logan_ms_per_slice": fbp_ms_per_slice,
                 "batch32_fp_adjoint_ms": fa_ms,
+                "batch32_adjoint_only_ms": adj_ms,
+                "adjoint_effective_gather_gbs": adj_gather_gbs,
                 "plain_batch32_fp_adjoint_ms": plain_ms,
                 "speedup_vs_plain": (plain_ms / fa_ms) if plain_ms else None,
                 "fp_samples_per_slice": plan.total_samples,

@@ -107,6 +107,7 @@ SIGNATURES = {
                                     _P(ctypes.c_float), _i, _P(CtPlanOpts), _P(_vp)]),
     "ct_plan_destroy": (_i, [_vp]),
     "ct_plan_check": (_i, [_vp]),
+    "ct_plan_selftest_wait_timeout": (_i, [_vp, ctypes.c_int32, _vp]),
     "ct_plan_geom": (_i, [_vp, _P(CtFanGeom)]),
     "ct_workspace_size": (_i, [_vp, _i, _i, _P(_sz)]),
     "ct_fp_fan": (_i, [_vp, _vp, _vp, _i, _vp, _sz, _vp]),

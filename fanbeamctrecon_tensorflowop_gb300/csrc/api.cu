@@ -345,6 +345,16 @@ ct_status ct_plan_check(const ct_plan *plan) {
     return CT_OK;
 }
 
+ct_status ct_plan_selftest_wait_timeout(const ct_plan *plan, int32_t budget_us,
+                                        ct_stream stream) {
+    if (!plan) return CT_ERR_NULL_POINTER;
+    if (budget_us < 1 || budget_us > 1000000) return CT_ERR_INVALID_ARGUMENT;
+    DeviceScope ds(plan->device);
+    if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
+    return launch_status(ctk::wait_selftest(plan, 1000ull * (unsigned long long)budget_us, stream),
+                         "ct_plan_selftest_wait_timeout");
+}
+
 ct_status ct_plan_geom(const ct_plan *plan, ct_fan_geom *out) {
     if (!plan || !out) return CT_ERR_NULL_POINTER;
     *out = plan->g;

@@ -33,7 +33,8 @@ constexpr int TC_THREADS = 128;
 constexpr unsigned TC_A_BYTES = TC_BM * TC_BK * 4;  // 16 KB
 constexpr unsigned TC_B_BYTES = TC_BN * TC_BK * 4;  // 28 KB
 constexpr unsigned TC_SMEM = 1024 /*align slack*/ + 3 * TC_A_BYTES + 2 * TC_B_BYTES + 64;
-constexpr long long TC_WAIT_LIMIT = 1ll << 26;
+// a wait gives up after this long (the waits of a healthy launch take microseconds)
+constexpr unsigned long long TC_WAIT_NS = 1000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -49,10 +50,19 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-// Bounded wait on phase `parity`; returns false after TC_WAIT_LIMIT polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait on phase `parity`: returns false once `budget_ns` nanoseconds
+// (of the global timer) have passed without the phase completing.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned long long budget_ns = TC_WAIT_NS) {
     const uint32_t a = smem_u32(bar);
-    for (long long it = 0; it < TC_WAIT_LIMIT; ++it) {
+    const unsigned long long t0 = global_ns();
+    for (;;) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -61,8 +71,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if (global_ns() - t0 > budget_ns) return false;
     }
-    return false;
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
@@ -274,7 +284,24 @@ bool make_map(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Exercises the timeout path of mbar_wait: one thread waits on a barrier
+// that nothing arrives at, gives up after budget_ns and raises `err`, as the
+// filter kernel does.
+__global__ void wait_selftest_kernel(int *err, unsigned long long budget_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait(&bar, 0, budget_ns)) atomicExch(err, 1);
+}
+
 }  // namespace
+
+int wait_selftest(const ct_plan *p, unsigned long long budget_ns, void *stream) {
+    wait_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(p->d_err, budget_ns);
+    ct_count_launch();
+    return (int)cudaGetLastError();
+}
 
 int tc_padded(int C) { return (C + TC_BN - 1) / TC_BN * TC_BN; }
 

@@ -101,6 +101,8 @@ int tc_padded(int C);
 bool ramp_tc_supported(int C);
 void build_tc_taps(const float *taps, int C, std::vector<float> &hi, std::vector<float> &lo);
 int ramp_filter_tc(const ct_plan *p, const float *in, float *out, int rows, void *stream);
+// One bounded wait that nothing completes; raises the plan's error flag.
+int wait_selftest(const ct_plan *p, unsigned long long budget_ns, void *stream);
 // Whether FBP / FDK weight the projections before filtering (short scan or
 // cosine pre-weighting).
 inline bool has_preweight(const ct_plan *p) { return p->d_parker || p->d_cosw; }

@@ -178,6 +178,12 @@ ct_status ct_plan_destroy(ct_plan *plan);
  * a kernel of this plan hit the iteration limit of one of its bounded waits
  * since the last check (only the tensor-core filter waits on barriers). */
 ct_status ct_plan_check(const ct_plan *plan);
+/* Failure-path self-test: enqueues one thread that waits, with the filter's
+ * bounded-wait code, on a barrier nothing completes, gives up after budget_us
+ * microseconds (1 .. 1,000,000) and raises the plan's error flag, so that the
+ * next ct_plan_check returns CT_ERR_TIMEOUT.  The context stays usable. */
+ct_status ct_plan_selftest_wait_timeout(const ct_plan *plan, int32_t budget_us,
+                                        ct_stream stream);
 /* The geometry a plan was built from. */
 ct_status ct_plan_geom(const ct_plan *plan, ct_fan_geom *out);
 

@@ -65,3 +65,24 @@ def test_tc_filter_rejects_unsupported_widths(cuda):
     p, a = G.small(cols=98)  # 98 % 4 != 0: TMA rows must be 16-byte multiples
     with pytest.raises(_lib.CtError):
         FanPlan(p, a, device=cuda, filter_algo=_lib.FILTER_TOEPLITZ_TC)
+
+
+def test_bounded_wait_timeout_is_reported_and_context_survives(cuda, orc):
+    """The filter's bounded mbarrier wait, on a barrier nothing completes, gives
+    up after its budget and raises the plan's flag; ct_plan_check reports it
+    once, and the context keeps working."""
+    p, a = G.small(n=40, views=36, cols=64)
+    tc = FanPlan(p, a, device=cuda, filter_algo=_lib.FILTER_TOEPLITZ_TC)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    assert lib.ct_plan_check(tc._h) == 0
+    assert lib.ct_plan_selftest_wait_timeout(tc._h, 20000, stream) == 0  # 20 ms budget
+    assert lib.ct_plan_check(tc._h) == 7  # CT_ERR_TIMEOUT
+    assert b"gave up" in lib.ct_last_error()
+    assert lib.ct_plan_check(tc._h) == 0  # reported once
+    assert lib.ct_plan_selftest_wait_timeout(tc._h, 0, stream) == 1
+    g = orc.decode(p)
+    y = np.random.default_rng(4).uniform(0, 1, (2, 36, 64)).astype(np.float32)
+    got = _np(tc.fbp(torch.from_numpy(y).to(cuda)))
+    assert rel_l2(got, orc.fbp_fan(g, a, y)) <= TOL
+    assert lib.ct_plan_check(tc._h) == 0
