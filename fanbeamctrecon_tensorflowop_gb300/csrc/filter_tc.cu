@@ -21,9 +21,15 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace ctk {
 namespace {
+
+using tma::mbar_expect_tx;
+using tma::mbar_init;
+using tma::mbar_wait;
+using tma::smem_u32;
 
 constexpr int TC_BM = 128;
 constexpr int TC_BN = 224;
@@ -33,47 +39,6 @@ constexpr int TC_THREADS = 128;
 constexpr unsigned TC_A_BYTES = TC_BM * TC_BK * 4;  // 16 KB
 constexpr unsigned TC_B_BYTES = TC_BN * TC_BK * 4;  // 28 KB
 constexpr unsigned TC_SMEM = 1024 /*align slack*/ + 3 * TC_A_BYTES + 2 * TC_B_BYTES + 64;
-// a wait gives up after this long (the waits of a healthy launch take microseconds)
-constexpr unsigned long long TC_WAIT_NS = 1000000000ull;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bounded wait on phase `parity`: returns false once `budget_ns` nanoseconds
-// (of the global timer) have passed without the phase completing.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
-                                          unsigned long long budget_ns = TC_WAIT_NS) {
-    const uint32_t a = smem_u32(bar);
-    const unsigned long long t0 = global_ns();
-    for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            " selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if (global_ns() - t0 > budget_ns) return false;
-    }
-}
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
                                             uint64_t *bar) {

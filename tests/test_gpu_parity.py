@@ -68,6 +68,21 @@ def test_fp(case, cuda, orc):
     assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
 
 
+@pytest.mark.parametrize("batch", [9, 20])
+def test_fp_staged_batches(case, cuda, orc, batch):
+    """Batches of 8+ slices walk 16 (then 8, 4, 1) slices at a time: slices
+    against the oracle (three of them) and against the slice projected alone."""
+    name, p, a, plan, _, g = case
+    x = _images(g, batch, seed=11)
+    got = _np(plan.fp(_t(x, cuda)))
+    pick = [0, batch // 2, batch - 1]
+    ref = orc.fp_fan(g, a, x[pick])
+    assert rel_l2(got[pick], ref) <= TOL, (name, rel_l2(got[pick], ref))
+    for k in pick:
+        alone = _np(plan.fp(_t(x[k:k + 1], cuda)))[0]
+        assert np.array_equal(got[k], alone), (name, k)
+
+
 def test_fp_adjoint(case, cuda, orc):
     name, p, a, plan, _, g = case
     y = _sinos(g, 2, seed=5)
@@ -308,7 +323,8 @@ def test_full_size_batch_properties(cuda):
     assert rel_l2(_np(f12), _np(2.0 * f1 - 3.0 * f2)) < 1e-5
     m = _dot_mismatch(_np(f1), _np(y), _np(x1), _np(plan.fp_adjoint(y)))
     assert m <= DOT_TOL, m
-    # slice b of a batch equals the slice alone
+    # slice b of a batch equals the slice alone (same arithmetic per slice
+    # whatever the number of slices per walk)
     assert torch.equal(plan.fp(x1[5:6])[0], f1[5])
     r = plan.fbp(y)
     assert torch.equal(plan.fbp(y[7:8])[0], r[7])
