@@ -12,6 +12,11 @@
 #include <climits>
 
 #include "cellwalk.cuh"
+#include "fp_body.cuh"
+
+#ifndef CT_CONE_FP_ROWS
+#define CT_CONE_FP_ROWS 8
+#endif
 
 namespace ctk {
 namespace {
@@ -201,36 +206,96 @@ __global__ void __launch_bounds__(kThreads)
 
 // ---- cone-beam forward projection -----------------------------------------------
 // Warp = 32 consecutive channels of one view, as in the fan-beam projector:
-// the warp walks its rays' in-plane cells row-synchronously (transposed
-// volume when most rays run along x) and, per lane, handles RB detector rows
-// at once.  Detector row r sits at height h_r = det_bottom + (r+1/2) drow on
-// the cylinder of radius D about the source; at in-plane distance s the ray
-// is at height z = z_s + h_r s / D (z_s the view's source height), so its z
-// cell coordinate is linear in the
-// sample index.  Inside an in-plane cell the bilinear weights are quadratic
-// and the z fraction linear in the sample index, so each (cell, row) sum is
-// exact in closed form from sum j^m, m <= 3 (split where the z cell changes).
+// the warp walks its rays' in-plane cells row-synchronously over quad images
+// of every slice (layout 0, or the transposed layout 1 when most rays run
+// along x) and, per lane, handles RB detector rows at once.  Detector row r
+// sits at height h_r = det_bottom + (r+1/2) drow on the cylinder of radius D
+// about the source; at in-plane distance s from the source the ray is at
+// height z = z_s + h_r s / D, so its z cell coordinate is w0 + dw k in the
+// sample index k.
+// Inside an in-plane cell the four bilinear weights are quadratics q_c(j) in
+// the sample offset j, and the z fraction is cz + dw j.  Per cell the walk
+// forms W_c = sum q_c(j) and M_c = sum j q_c(j) once (from sum j^m, m <= 3);
+// a detector row whose z cell does not change inside the cell (all but a few
+// percent) then adds
+//   sum_c [(W_c (1 - cz) - dw M_c) t0_c + (W_c cz + dw M_c) t1_c]
+// with t0, t1 the cell's quads of slices kz and kz+1 (two 16-byte loads).
+// A row that crosses a z boundary inside the cell sums the pieces the same
+// way with W_c and M_c over each piece's offsets, in an out-of-line function
+// (inlined into every unrolled row it made the kernel too large for the
+// instruction cache).
 // Weight: 0.125*dx*sqrt(1 + (h_r/D)^2), the 3-D length of one in-plane step.
 struct ConeFpArgs {
-    int V, C, nx, ny, nz, n_rows, wpv;
+    int V, C, nx, nz, n_rows, wpv;
     float w;        // 0.125*dx
     float D, det_bottom, drow, dz, zmin;
     int max_iter;
 };
 
+// sum over j in [js, je) of j^0..j^3
+__device__ __forceinline__ void power_sums(float js, float je, float &S0, float &S1, float &S2,
+                                           float &S3) {
+    auto p1 = [](float n) { return 0.5f * n * (n + 1.0f); };  // sum_{0..n} j
+    auto p2 = [](float n) { return n * (n + 1.0f) * (2.0f * n + 1.0f) * (1.0f / 6.0f); };
+    S0 = je - js;
+    S1 = p1(je - 1.0f) - p1(js - 1.0f);
+    S2 = p2(je - 1.0f) - p2(js - 1.0f);
+    const float a = p1(je - 1.0f), b = p1(js - 1.0f);
+    S3 = a * a - b * b;
+}
+
+__device__ __forceinline__ float dot4(float4 a, float4 t) {
+    return fmaf(a.x, t.x, fmaf(a.y, t.y, fmaf(a.z, t.z, a.w * t.w)));
+}
+
+// moments sum q_c(j) j^m over a piece, from its power sums: c0 S_m + c1 S_{m+1} + c2 S_{m+2}
+__device__ __forceinline__ float4 moment(float4 c0, float4 c1, float4 c2, float Sa, float Sb,
+                                         float Sc) {
+    return make_float4(fmaf(c0.x, Sa, fmaf(c1.x, Sb, c2.x * Sc)),
+                       fmaf(c0.y, Sa, fmaf(c1.y, Sb, c2.y * Sc)),
+                       fmaf(c0.z, Sa, fmaf(c1.z, Sb, c2.z * Sc)),
+                       fmaf(c0.w, Sa, fmaf(c1.w, Sb, c2.w * Sc)));
+}
+
+// One detector row's sum over a cell whose samples cross z cell boundaries:
+// the z cell coordinate is wk + dw j for the j-th of the cell's cnt samples.
+__device__ __noinline__ float cone_row_pieces(float4 c0, float4 c1, float4 c2,
+                                              const float4 *__restrict__ qc, size_t slice_stride,
+                                              int nz, float wk, float dw, float cnt) {
+    float acc = 0.0f, js = 0.0f;
+    for (int t = 0; t < 16 && js < cnt; ++t) {  // every piece has >= 1 sample
+        const float kzp = floorf(fmaf(dw, js, wk));
+        float je = cnt;
+        if (dw > 0.0f) je = fminf(cnt, ceilf((kzp + 1.0f - wk) / dw));
+        else if (dw < 0.0f) je = fminf(cnt, ceilf((kzp - wk) / dw));
+        if (!(je > js)) je = js + 1.0f;  // always progress
+        float P0, P1, P2, P3;
+        power_sums(js, je, P0, P1, P2, P3);
+        const float4 W = moment(c0, c1, c2, P0, P1, P2), M = moment(c0, c1, c2, P1, P2, P3);
+        const float cz = wk - kzp;  // z fraction cz + dw j on this piece
+        const int z0 = min(max((int)kzp, 0), nz - 1), z1 = min(max((int)kzp + 1, 0), nz - 1);
+        const float4 t0 = __ldg(qc + (size_t)z0 * slice_stride);
+        const float4 t1 = __ldg(qc + (size_t)z1 * slice_stride);
+        const float4 B = make_float4(fmaf(W.x, cz, dw * M.x), fmaf(W.y, cz, dw * M.y),
+                                     fmaf(W.z, cz, dw * M.z), fmaf(W.w, cz, dw * M.w));
+        const float4 A = make_float4(W.x - B.x, W.y - B.y, W.z - B.z, W.w - B.w);
+        acc += dot4(A, t0) + dot4(B, t1);
+        js = je;
+    }
+    return acc;
+}
+
 template <int RB>
 __global__ void __launch_bounds__(kThreads)
-    cone_fp_kernel(const float *__restrict__ vol, const float *__restrict__ vol_t,
-                   float *__restrict__ proj, const float4 *__restrict__ ray,
-                   const int *__restrict__ nsamp, const float2 *__restrict__ chan_s,
-                   const float *__restrict__ view_z, ConeFpArgs a, int batch) {
+    cone_fp_kernel(const float4 *__restrict__ quads, float *__restrict__ proj,
+                   const float4 *__restrict__ ray, const int *__restrict__ nsamp,
+                   const float2 *__restrict__ chan_s, const float *__restrict__ view_z,
+                   ConeFpArgs a) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
-    if (gw >= a.V * a.wpv) return;
-    const int rgroups = (a.n_rows + RB - 1) / RB;
-    const int b = blockIdx.y / rgroups;
-    const int r0 = (blockIdx.y - b * rgroups) * RB;
+    if (gw >= a.V * a.wpv) return;  // warp-uniform
+    const int r0 = blockIdx.y * RB;
     const int v = gw / a.wpv;
     const int c = (gw - v * a.wpv) * 32 + lane;
     const bool has_c = c < a.C;
@@ -243,11 +308,12 @@ __global__ void __launch_bounds__(kThreads)
     const bool along_x = 2 * __popc(xm) > __popc(vm);
     const RaySeg seg = along_x ? RaySeg{q.y - 0.5f, q.x - 0.5f, q.w, q.z}
                                : RaySeg{q.x - 0.5f, q.y - 0.5f, q.z, q.w};
-    const int W = along_x ? a.ny : a.nx, H = along_x ? a.nx : a.ny;
-    const size_t plane = (size_t)a.nx * a.ny;
-    const float *vb = (along_x ? vol_t : vol) + (size_t)min(b, batch - 1) * a.nz * plane;
-    // z cell coordinate of sample k for row rr: w0[rr] + dw[rr] * k
-    // in-plane distance from the source of sample k: s0 - k * chord / n (mm)
+    const int Q = a.nx + 1;
+    const size_t lsz = (size_t)Q * Q, sstride = 2 * lsz;
+    // slice k's quads of this warp's layout: ql + k * 2 lsz
+    const float4 *ql = quads + (along_x ? lsz : 0);
+    // z cell coordinate of sample k for row rr: w0[rr] + dw[rr] * k; in-plane
+    // distance from the source of sample k: s0 - k * chord / n (mm)
     const float2 sd = has_c ? __ldg(chan_s + c) : make_float2(0.f, 0.f);
     const float ds = valid ? -sd.y / (float)n : 0.0f;
     const float zs = view_z ? __ldg(view_z + v) : 0.0f;
@@ -259,60 +325,37 @@ __global__ void __launch_bounds__(kThreads)
         dw[rr] = h * ds / (a.D * a.dz);
         acc[rr] = 0.0f;
     }
-    // adds the closed-form sums of cell (cu, cv) for samples k .. k+cnt-1
+    // adds the cell (cu, cv) holding samples k .. k+cnt-1 with entry fractions fa, fb
     auto cell = [&](int cu, int cv, float cnt, float fa, float fb, float k) {
         // bilinear weights as quadratics in j: (1-fu)(1-fv), fu(1-fv), (1-fu)fv, fu fv
-        const float Au = 1.0f - fa, Av = 1.0f - fb;
-        const float q00[3] = {Au * Av, -(Au * seg.sv + Av * seg.su), seg.su * seg.sv};
-        const float q10[3] = {fa * Av, seg.su * Av - fa * seg.sv, -seg.su * seg.sv};
-        const float q01[3] = {Au * fb, Au * seg.sv - seg.su * fb, -seg.su * seg.sv};
-        const float q11[3] = {fa * fb, fa * seg.sv + fb * seg.su, seg.su * seg.sv};
-        const int i0 = min(max(cu, 0), W - 1), i1 = min(max(cu + 1, 0), W - 1);
-        const int j0 = min(max(cv, 0), H - 1) * W, j1 = min(max(cv + 1, 0), H - 1) * W;
+        const float Au = 1.0f - fa, Av = 1.0f - fb, uv = seg.su * seg.sv;
+        const float4 c0 = make_float4(Au * Av, fa * Av, Au * fb, fa * fb);
+        const float4 c1 = make_float4(-(Au * seg.sv + Av * seg.su), seg.su * Av - fa * seg.sv,
+                                      Au * seg.sv - seg.su * fb, fa * seg.sv + fb * seg.su);
+        const float4 c2 = make_float4(uv, -uv, -uv, uv);
+        const int qi = min(max(cu + 1, 0), Q - 1), qj = min(max(cv + 1, 0), Q - 1);
+        const float4 *qc = ql + (size_t)qj * Q + qi;
+        float S0, S1, S2, S3;
+        power_sums(0.0f, cnt, S0, S1, S2, S3);
+        const float4 W = moment(c0, c1, c2, S0, S1, S2), M = moment(c0, c1, c2, S1, S2, S3);
 #pragma unroll
         for (int rr = 0; rr < RB; ++rr) {
             if (r0 + rr >= a.n_rows) break;
-            // z cells inside this cell's samples: split where floor(w) changes
-            float kk = k;
-            const float kend = k + cnt;
-            for (int t = 0; t < 16 && kk < kend; ++t) {  // every piece has >= 1 sample
-                const float wk = fmaf(dw[rr], kk, w0[rr]);
-                const float kz = floorf(wk);
-                // next z boundary in sample units
-                float kb = kend;
-                if (dw[rr] > 0.0f) kb = fminf(kend, ceilf((kz + 1.0f - w0[rr]) / dw[rr]));
-                else if (dw[rr] < 0.0f) kb = fminf(kend, ceilf((kz - w0[rr]) / dw[rr]));
-                if (!(kb > kk)) kb = kk + 1.0f;  // always progress
-                const float n_ = kb - kk;
-                const float j0f = kk - k;  // offset of this piece inside the cell
-                // sums over j = j0f .. j0f + n_ - 1
-                const float e = j0f + n_ - 1.0f;
-                const float S0 = n_;
-                const float S1 = 0.5f * (j0f + e) * n_;
-                // sum j^2 and j^3 over [j0f, e] from prefix formulas
-                const float P2e = e * (e + 1.0f) * (2.0f * e + 1.0f) * (1.0f / 6.0f);
-                const float P2s = (j0f - 1.0f) * j0f * (2.0f * j0f - 1.0f) * (1.0f / 6.0f);
-                const float P3e = 0.25f * e * e * (e + 1.0f) * (e + 1.0f);
-                const float P3s = 0.25f * (j0f - 1.0f) * (j0f - 1.0f) * j0f * j0f;
-                const float S2 = P2e - P2s, S3 = P3e - P3s;
-                // z fraction as a linear function of j: cz + dz_ j
-                const float cz = fmaf(dw[rr], k, w0[rr]) - kz;
-                const float dzj = dw[rr];
-                const int z0 = min(max((int)kz, 0), a.nz - 1), z1 = min(max((int)kz + 1, 0), a.nz - 1);
-                const float *p0 = vb + (size_t)z0 * plane, *p1 = vb + (size_t)z1 * plane;
-                const float t00[2] = {__ldg(p0 + j0 + i0), __ldg(p1 + j0 + i0)};
-                const float t10[2] = {__ldg(p0 + j0 + i1), __ldg(p1 + j0 + i1)};
-                const float t01[2] = {__ldg(p0 + j1 + i0), __ldg(p1 + j1 + i0)};
-                const float t11[2] = {__ldg(p0 + j1 + i1), __ldg(p1 + j1 + i1)};
-                auto sum2 = [&](const float *qq, const float *tt) {
-                    const float sq = qq[0] * S0 + qq[1] * S1 + qq[2] * S2;      // sum Q
-                    const float sqz = qq[0] * cz * S0 + (qq[0] * dzj + qq[1] * cz) * S1 +
-                                      (qq[1] * dzj + qq[2] * cz) * S2 + qq[2] * dzj * S3;  // sum Q fz
-                    return fmaf(sq - sqz, tt[0], sqz * tt[1]);
-                };
-                acc[rr] += sum2(q00, t00) + sum2(q10, t10) + sum2(q01, t01) + sum2(q11, t11);
-                kk = kb;
+            const float wk = fmaf(dw[rr], k, w0[rr]);
+            const float kz = floorf(wk);
+            if (kz != floorf(fmaf(dw[rr], cnt - 1.0f, wk))) {
+                acc[rr] += cone_row_pieces(c0, c1, c2, qc, sstride, a.nz, wk, dw[rr], cnt);
+                continue;
             }
+            const float cz = wk - kz, d = dw[rr];
+            const int z0 = min(max((int)kz, 0), a.nz - 1);
+            const int z1 = min(max((int)kz + 1, 0), a.nz - 1);
+            const float4 t0 = __ldg(qc + (size_t)z0 * sstride);
+            const float4 t1 = __ldg(qc + (size_t)z1 * sstride);
+            const float4 B = make_float4(fmaf(W.x, cz, d * M.x), fmaf(W.y, cz, d * M.y),
+                                         fmaf(W.z, cz, d * M.z), fmaf(W.w, cz, d * M.w));
+            const float4 A = make_float4(W.x - B.x, W.y - B.y, W.z - B.z, W.w - B.w);
+            acc[rr] += dot4(A, t0) + dot4(B, t1);
         }
     };
     const unsigned pm = __ballot_sync(FULL, valid && seg.sv > 0.0f);
@@ -368,8 +411,8 @@ __global__ void __launch_bounds__(kThreads)
             cell(cu, cv, cnt, fa, fb, kf);
         });
     }
-    if (has_c && b < batch) {
-        float *pv = proj + ((size_t)b * a.V + v) * a.n_rows * a.C;
+    if (has_c) {
+        float *pv = proj + (size_t)v * a.n_rows * a.C;
 #pragma unroll
         for (int rr = 0; rr < RB; ++rr) {
             if (r0 + rr >= a.n_rows) break;
@@ -379,23 +422,18 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// in [nz][ny][nx] planes -> out [nz][nx][ny]
+// Quad images of every slice of one volume ([nz][2 layouts][(nx+1)^2]), as the
+// fan-beam projector builds them per slice.
 __global__ void __launch_bounds__(256)
-    transpose_planes_kernel(const float *__restrict__ in, float *__restrict__ out, int nx, int ny) {
-    __shared__ float t[32][33];
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
-    const size_t plane = (size_t)nx * ny;
-    const float *src = in + blockIdx.z * plane;
-    float *dst = out + blockIdx.z * plane;
-    for (int j = threadIdx.y; j < 32; j += 8) {
-        const int x = x0 + threadIdx.x, y = y0 + j;
-        if (x < nx && y < ny) t[j][threadIdx.x] = src[(size_t)y * nx + x];
-    }
-    __syncthreads();
-    for (int j = threadIdx.y; j < 32; j += 8) {
-        const int y = y0 + threadIdx.x, x = x0 + j;
-        if (x < nx && y < ny) dst[(size_t)x * ny + y] = t[threadIdx.x][j];
-    }
+    cone_quads_kernel(const float *__restrict__ vol, float4 *__restrict__ quads, int nx,
+                      int ny) {
+    const int Q = nx + 1;
+    const int qi = blockIdx.x * 32 + threadIdx.x, qj = blockIdx.y * 8 + threadIdx.y;
+    if (qi >= Q || qj >= Q) return;
+    const int layout = blockIdx.z & 1, k = blockIdx.z >> 1;
+    build_quad(vol + (size_t)k * nx * ny,
+               quads + ((size_t)k * 2 + layout) * Q * Q + (size_t)qj * Q + qi, nx, ny, layout,
+               qi, qj);
 }
 
 ConeArgs make_cone_args(const ct_plan *p) {
@@ -473,24 +511,20 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
 }
 
 size_t cone_fp_work_bytes(const ct_plan *p, int batch) {
-    return sizeof(float) * (size_t)batch * p->nz * p->g.nx * p->g.ny;
+    // the quad images of one volume at a time
+    (void)batch;
+    return sizeof(float4) * 2 * (size_t)p->nz * (p->g.nx + 1) * (p->g.nx + 1);
 }
 
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work,
             void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     const int nx = p->g.nx, ny = p->g.ny, nz = p->nz;
-    float *vol_t = static_cast<float *>(work);
-    for (int b0 = 0; b0 < batch; ++b0) {
-        transpose_planes_kernel<<<dim3((nx + 31) / 32, (ny + 31) / 32, nz), dim3(32, 8), 0, s>>>(
-            vol + (size_t)b0 * nz * nx * ny, vol_t + (size_t)b0 * nz * nx * ny, nx, ny);
-        ct_count_launch();
-    }
+    float4 *quads = static_cast<float4 *>(work);
     ConeFpArgs a;
     a.V = p->g.n_views;
     a.C = p->g.n_cols;
     a.nx = nx;
-    a.ny = ny;
     a.nz = nz;
     a.n_rows = p->n_rows;
     a.wpv = (a.C + 31) / 32;
@@ -501,17 +535,18 @@ int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *wo
     a.dz = p->g.dz;
     a.zmin = -0.5f * p->g.dz * (float)nz;
     a.max_iter = 2 * (nx > ny ? nx : ny) + 8;
-    constexpr int RB = 8;
+    constexpr int RB = CT_CONE_FP_ROWS;
     const int rgroups = (a.n_rows + RB - 1) / RB;
     const int blocks = (a.V * a.wpv + kThreads / 32 - 1) / (kThreads / 32);
-    const int per = 65535 / rgroups;
-    for (int b0 = 0; b0 < batch; b0 += per) {
-        const int nb = batch - b0 < per ? batch - b0 : per;
-        cone_fp_kernel<RB><<<dim3(blocks, rgroups * nb), kThreads, 0, s>>>(
-            vol + (size_t)b0 * nz * nx * ny, vol_t + (size_t)b0 * nz * nx * ny,
-            proj + (size_t)b0 * a.V * a.n_rows * a.C, reinterpret_cast<const float4 *>(p->d_ray),
-            p->d_nsamp, reinterpret_cast<const float2 *>(p->d_chan_s), p->d_view_z, a, nb);
-        ct_count_launch();
+    const int Q = nx + 1;
+    for (int b = 0; b < batch; ++b) {
+        cone_quads_kernel<<<dim3((Q + 31) / 32, (Q + 7) / 8, 2 * nz), dim3(32, 8), 0, s>>>(
+            vol + (size_t)b * nz * nx * ny, quads, nx, ny);
+        cone_fp_kernel<RB><<<dim3(blocks, rgroups), kThreads, 0, s>>>(
+            quads, proj + (size_t)b * a.V * a.n_rows * a.C,
+            reinterpret_cast<const float4 *>(p->d_ray), p->d_nsamp,
+            reinterpret_cast<const float2 *>(p->d_chan_s), p->d_view_z, a);
+        ct_count_launch(2);
     }
     return (int)cudaGetLastError();
 }

@@ -5,7 +5,9 @@
 Geometry: 512x512 at 0.7 mm, 984 views x 888 channels (1 mm pitch at the
 detector), SID 541 / SDD 949 mm.  One untimed warm-up call precedes the
 ``iters`` profiled calls, so ``ncu -s <launches of one call>`` skips it.
-Ops: fp, fp_adjoint, bp, bp_adjoint, filter, fbp, fbp_adjoint.
+Ops: fp, fp_adjoint, bp, bp_adjoint, filter, fbp, fbp_adjoint; cone_fp, fdk and
+fdk_adjoint take ``--batch`` volumes of 512^2 x 64 voxels (0.7 x 0.7 x 0.625 mm) with
+888 x 64 detector cells (1 mm rows) per view.
 """
 from __future__ import annotations
 
@@ -16,7 +18,7 @@ import torch
 
 from . import _lib, phantom
 from .geometry import angle, fan_param16
-from .ops import FanPlan
+from .ops import ConePlan, FanPlan
 
 
 def main() -> None:
@@ -35,6 +37,24 @@ def main() -> None:
                     pixel_mm=args.pixel, dcol_rad=1.0 / 949.0)
     a = angle(args.views, 0.0)
     win = _lib.WINDOW_RAMLAK if args.window == "ramlak" else _lib.WINDOW_SHEPP_LOGAN
+    if args.op in ("cone_fp", "fdk", "fdk_adjoint"):
+        n_rows = nz = 64
+        pc = fan_param16(sdd=949.0, sid=541.0, n_views=args.views, n_cols=args.cols, n=args.n,
+                         pixel_mm=args.pixel, dcol_rad=1.0 / 949.0, det_bottom=-n_rows / 2.0,
+                         drow=1.0, dz=0.625)
+        cplan = ConePlan(pc, angle(args.views, 0.0), n_rows, nz, device=dev)
+        vol = torch.rand((args.batch, nz, args.n, args.n), device=dev)
+        proj = cplan.fp_cone(vol)
+        fn = {"cone_fp": lambda: cplan.fp_cone(vol, out=proj),
+              "fdk": lambda: cplan.fdk(proj),
+              "fdk_adjoint": lambda: cplan.fdk_adjoint(vol)}[args.op]
+        fn()
+        torch.cuda.synchronize()
+        for _ in range(args.iters):
+            fn()
+        torch.cuda.synchronize()
+        print(f"profile_case {args.op} batch={args.batch} ok")
+        return
     plan = FanPlan(p, a, device=dev, window=win)
     img = torch.from_numpy(np.stack([phantom.ellipse_phantom(args.n, args.pixel, seed=s)
                                      for s in range(args.batch)])).to(dev)
