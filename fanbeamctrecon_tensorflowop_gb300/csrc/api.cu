@@ -87,8 +87,9 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
         case CT_OP_FP_CONE:
             return ctk::cone_fp_work_bytes(p, batch);
         case CT_OP_FDK_CONE:
-        case CT_OP_FDK_CONE_ADJOINT:
             return parker * proj_bytes(p, batch);
+        case CT_OP_FDK_CONE_ADJOINT:  // + the transpose's per-volume maxima
+            return parker * proj_bytes(p, batch) + ctk::cone_bp_transpose_work_bytes(batch);
         case CT_OP_FP:
             return ctk::fp_fan_work_bytes(p, batch);
         case CT_OP_FP_ADJOINT:
@@ -525,7 +526,7 @@ ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_
     if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
         ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
         return CT_ERR_UNSUPPORTED;
-    if (sizeof(float) * 16 * (size_t)plan->g.n_cols > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    if (!ctk::cone_bp_transpose_supported(plan)) return CT_ERR_UNSUPPORTED;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     Workspace w;
@@ -533,7 +534,9 @@ ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_
                  stream);
     if (st != CT_OK) return st;
     float *tmp = static_cast<float *>(w.ptr);
-    st = launch_status(ctk::cone_bp_transpose(plan, d_vol, tmp, batch, stream),
+    void *maxima = static_cast<char *>(w.ptr) + (ctk::has_preweight(plan) ? 2 : 1) *
+                                                    proj_bytes(plan, batch);
+    st = launch_status(ctk::cone_bp_transpose(plan, d_vol, tmp, batch, maxima, stream),
                        "ct_fdk_cone_adjoint");
     if (st != CT_OK) return st;
     const int rows = batch * plan->g.n_views * plan->n_rows;

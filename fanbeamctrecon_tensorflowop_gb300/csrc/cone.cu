@@ -33,6 +33,8 @@ struct ConeArgs {
     double fov_r2;
     float coef[9];
     int atan_deg;
+    // fixed-point bounds of the transpose (see cone_bp_transpose_kernel)
+    float fix_npix, fix_slices, fix_wmax;
 };
 
 template <int DEG>
@@ -130,28 +132,60 @@ __global__ void __launch_bounds__(kThreads)
 // the view accumulate in shared memory.  Threads sweep the FOV pixels; for
 // each they compute column, weight and row slope once and visit only the z
 // slices whose row coordinate reaches the block's rows.
+// The accumulation is in 32-bit fixed point: FP32 shared-memory atomicAdd is
+// a compare-and-swap loop on this GPU, int32 atomicAdd is native.  Every
+// contribution is at most max|vol| * w_max (w = 1/L^2, L >= R - rFOV; the
+// bilinear weights are <= 1), and a detector cell receives at most npix
+// (pixels within two channels of it) x slices (within one row of it) of them,
+// so with scale = 2^30 / (npix * slices * max|vol| * w_max) no sum can
+// overflow; each contribution is rounded to 1/scale.  Samples whose row
+// coordinate is clamped onto the first or last row (slices beyond the
+// detector's reach, which can pile up there from every slice) add into two
+// separate fixed-point rows whose bound counts all nz slices, so they do not
+// coarsen the others.
 constexpr int kRB = 16;
+#ifndef CT_CONE_T_TILES
+#define CT_CONE_T_TILES 1
+#endif
 
 template <int DEG>
 __global__ void __launch_bounds__(kThreads)
     cone_bp_transpose_kernel(const float *__restrict__ vol, float *__restrict__ proj,
                              const float2 *__restrict__ view_cs, const float *__restrict__ view_z,
-                             ConeArgs a, int batch) {
-    extern __shared__ float rows_acc[];  // [kRB][C]
+                             const int *__restrict__ vmax_bits, ConeArgs a, int batch) {
+    // [kRB][C] fixed point, then [2][C]: the first and the last detector row's
+    // clamped samples, fixed point at their own scale
+    extern __shared__ int rows_acc[];
+    int *rows_clamped = rows_acc + kRB * a.C;
     const int rblocks = (a.n_rows + kRB - 1) / kRB;
     const int v = blockIdx.x;
     const int rb = blockIdx.y % rblocks, b = blockIdx.y / rblocks;
     const int R0 = rb * kRB;
     const int nr = min(kRB, a.n_rows - R0);
-    for (int k = threadIdx.x; k < kRB * a.C; k += kThreads) rows_acc[k] = 0.0f;
+    for (int k = threadIdx.x; k < (kRB + 2) * a.C; k += kThreads) rows_acc[k] = 0;
+    const float vmax = __int_as_float(__ldg(vmax_bits + b));
+    const float bound = a.fix_npix * a.fix_slices * a.fix_wmax * vmax;
+    const float scale = bound > 0.0f ? 1073741824.0f / bound : 0.0f;
+    const float bound_c = a.fix_npix * (float)a.nz * a.fix_wmax * vmax;
+    const float scale_c = bound_c > 0.0f ? 1073741824.0f / bound_c : 0.0f;
     __syncthreads();
     const float2 cs = __ldg(view_cs + v);
     const float zfirst = a.zmin + 0.5f * a.dz - (view_z ? __ldg(view_z + v) : 0.0f);
     const float *vb = vol + (size_t)b * a.nz * a.ny * a.nx;
     const float rmax = (float)a.n_rows;
     const size_t plane = (size_t)a.nx * a.ny;
-    for (int p = threadIdx.x; p < a.nx * a.ny; p += kThreads) {
-        const int iy = p / a.nx, ix = p - iy * a.nx;
+    // a warp takes a 4 x 8 pixel tile whose short side runs along the view's
+    // rays: pixels along a ray share detector columns, so the lanes of a warp
+    // spread over 8 columns instead of competing for a few
+    const bool along_x = fabsf(cs.x) > fabsf(cs.y);
+    const int tw = CT_CONE_T_TILES ? (along_x ? 4 : 8) : 32, th = 32 / tw;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ntx = (a.nx + tw - 1) / tw, ntiles = ntx * ((a.ny + th - 1) / th);
+    for (int tile = warp; tile < ntiles; tile += kThreads / 32) {
+        const int ty = tile / ntx, tx = tile - ty * ntx;
+        const int ix = tx * tw + lane % tw, iy = ty * th + lane / tw;
+        if (ix >= a.nx || iy >= a.ny) continue;
+        const int p = iy * a.nx + ix;
         const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
         const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
         if (!(xd * xd + yd * yd <= a.fov_r2)) continue;
@@ -189,19 +223,51 @@ __global__ void __launch_bounds__(kThreads)
             split_pos(rr, ir, fr);
             const int r0 = min(max(ir - 1, 0), a.n_rows - 1) - R0;
             const int r1 = min(ir, a.n_rows - 1) - R0;
+            if (ir < 1 || ir >= a.n_rows) {
+                // clamped onto an edge row: both row taps are that row
+                const int e = ir < 1 ? 0 : 1, re = e ? a.n_rows - 1 : 0;
+                if ((unsigned)(re - R0) < (unsigned)nr) {
+                    const float vc = val * scale_c;
+                    atomicAdd(&rows_clamped[e * a.C + i0], __float2int_rn(vc * (1.0f - f)));
+                    atomicAdd(&rows_clamped[e * a.C + i1], __float2int_rn(vc * f));
+                }
+                continue;
+            }
+            const float vs = val * scale;
             if ((unsigned)r0 < (unsigned)nr) {
-                atomicAdd(&rows_acc[r0 * a.C + i0], val * (1.0f - fr) * (1.0f - f));
-                atomicAdd(&rows_acc[r0 * a.C + i1], val * (1.0f - fr) * f);
+                atomicAdd(&rows_acc[r0 * a.C + i0], __float2int_rn(vs * (1.0f - fr) * (1.0f - f)));
+                atomicAdd(&rows_acc[r0 * a.C + i1], __float2int_rn(vs * (1.0f - fr) * f));
             }
             if ((unsigned)r1 < (unsigned)nr) {
-                atomicAdd(&rows_acc[r1 * a.C + i0], val * fr * (1.0f - f));
-                atomicAdd(&rows_acc[r1 * a.C + i1], val * fr * f);
+                atomicAdd(&rows_acc[r1 * a.C + i0], __float2int_rn(vs * fr * (1.0f - f)));
+                atomicAdd(&rows_acc[r1 * a.C + i1], __float2int_rn(vs * fr * f));
             }
         }
     }
     __syncthreads();
     float *pv = proj + ((size_t)b * a.V + v) * a.n_rows * a.C;
-    for (int k = threadIdx.x; k < nr * a.C; k += kThreads) pv[(size_t)R0 * a.C + k] = rows_acc[k];
+    const float inv = scale > 0.0f ? bound * (1.0f / 1073741824.0f) : 0.0f;
+    const float inv_c = scale_c > 0.0f ? bound_c * (1.0f / 1073741824.0f) : 0.0f;
+    for (int k = threadIdx.x; k < nr * a.C; k += kThreads) {
+        const int row = R0 + k / a.C, col = k - (k / a.C) * a.C;
+        float c = 0.0f;
+        if (row == 0) c += (float)rows_clamped[col] * inv_c;
+        if (row == a.n_rows - 1) c += (float)rows_clamped[a.C + col] * inv_c;
+        pv[(size_t)R0 * a.C + k] = fmaf((float)rows_acc[k], inv, c);
+    }
+}
+
+// vmax_bits[b] = bits of max |vol[b]| (non-negative floats order as their bits);
+// vmax_bits must start at zero.
+__global__ void __launch_bounds__(256)
+    volume_absmax_kernel(const float *__restrict__ vol, size_t per_volume, int *vmax_bits) {
+    const float *vb = vol + (size_t)blockIdx.y * per_volume;
+    float m = 0.0f;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < per_volume;
+         e += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(__ldg(vb + e)));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(vmax_bits + blockIdx.y, __float_as_int(m));
 }
 
 // ---- cone-beam forward projection -----------------------------------------------
@@ -488,10 +554,36 @@ int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *st
     return (int)cudaGetLastError();
 }
 
-int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream) {
-    const ConeArgs a = make_cone_args(p);
+size_t cone_bp_transpose_work_bytes(int batch) { return sizeof(int) * (size_t)batch; }
+
+bool cone_bp_transpose_supported(const ct_plan *p) {
+    return sizeof(int) * (kRB + 2) * (size_t)p->g.n_cols <= 227 * 1024;
+}
+
+int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *work,
+                      void *stream) {
+    ConeArgs a = make_cone_args(p);
+    {
+        // in pixels of the smaller pitch and in slices; mm otherwise
+        const double pix = p->g.dx < p->g.dy ? p->g.dx : p->g.dy;
+        const double R = p->g.sid, rf = p->g.rfov, D = p->g.sdd;
+        // pixel centres within two channels of a column: a wedge 2 dcol L wide
+        const double width = 2.0 * (double)p->g.dcol * (R + rf) / pix + 2.0;
+        const double length = 2.0 * rf / pix + 2.0;
+        a.fix_npix = (float)(width * length);
+        // slice centres within one row (drow L / D at the detector) either side
+        a.fix_slices = (float)(2.0 * (double)p->g.drow * (R + rf) / (D * (double)p->g.dz) + 2.0);
+        a.fix_wmax = (float)(1.0 / ((R - rf) * (R - rf)));
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int *vmax_bits = static_cast<int *>(work);
+    cudaError_t e0 = cudaMemsetAsync(vmax_bits, 0, sizeof(int) * (size_t)batch, s);
+    if (e0 != cudaSuccess) return (int)e0;
+    const size_t per_volume = (size_t)a.nz * a.ny * a.nx;
+    volume_absmax_kernel<<<dim3(152, batch), 256, 0, s>>>(vol, per_volume, vmax_bits);
+    ct_count_launch();
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
-    const size_t smem = sizeof(float) * kRB * a.C;
+    const size_t smem = sizeof(int) * (kRB + 2) * a.C;
     auto kern = a.atan_deg == 4   ? cone_bp_transpose_kernel<4>
                 : a.atan_deg == 8 ? cone_bp_transpose_kernel<8>
                                   : cone_bp_transpose_kernel<0>;
@@ -504,7 +596,7 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
         const int nb = batch - b0 < per ? batch - b0 : per;
         kern<<<dim3(a.V, rblocks * nb), kThreads, smem, (cudaStream_t)stream>>>(
             vol + (size_t)b0 * a.nz * a.ny * a.nx, proj + (size_t)b0 * a.V * a.n_rows * a.C, vcs,
-            p->d_view_z, a, nb);
+            p->d_view_z, vmax_bits + b0, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();

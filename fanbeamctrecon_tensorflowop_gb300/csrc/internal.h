@@ -110,7 +110,11 @@ inline bool has_preweight(const ct_plan *p) { return p->d_parker || p->d_cosw; }
 // [batch][V][n_rows][C]
 int apply_preweight(const ct_plan *p, const float *in, float *out, int batch, void *stream);
 int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream);
-int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *stream);
+// work: cone_bp_transpose_work_bytes(batch) bytes (per-volume max |vol|)
+size_t cone_bp_transpose_work_bytes(int batch);
+bool cone_bp_transpose_supported(const ct_plan *p);  // its detector rows fit in shared memory
+int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *work,
+                      void *stream);
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work, void *stream);
 size_t cone_fp_work_bytes(const ct_plan *p, int batch);
 ct_status batch_workspace(const ct_batch_item *items, int n, size_t *bytes);
