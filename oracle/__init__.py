@@ -4,9 +4,12 @@ TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
 CPU-baseline legs of ``bench.py`` import this package, and only as the checker
 or the timed CPU reference; the product path never calls it.
 
-Parity status: unpinned against reference outputs (the reference cannot be
-built and has no golden vectors); pinned to the reference's executed Python
-geometry packing and to exact / analytic known answers (see ``oracle.c``).
+Parity status: pinned to the reference's own ops, executed.  Its TensorFlow op
+wrappers and CUDA sources are compiled for the host against stand-ins
+(``build_ref.py``, ``refexec/``) and run by ``reference.py``; their outputs are
+the golden vectors in ``tests/golden/reference_ops.npz``.  With the GPU
+texture unit's weights (``texture_rule.h``, measured on GB300) this oracle
+meets them within 2e-6 (FP), 1e-6 (BP) and 5e-5 (FBP, FDK) relative L2.
 
 The C restatement (``oracle.c``) is compiled with gcc + OpenMP into
 ``oracle/_build/liboracle.so`` on first use (``build()``).
@@ -50,7 +53,8 @@ def build(force: bool = False) -> Path:
     """Compiles liboracle.so (gcc, OpenMP) if missing or stale."""
     _BUILD.mkdir(parents=True, exist_ok=True)
     stamp = _BUILD / "stamp.txt"
-    fp = hashlib.sha256(_SRC.read_bytes() + " ".join(_CFLAGS).encode()
+    fp = hashlib.sha256(_SRC.read_bytes() + (_SRC.parent / "texture_rule.h").read_bytes()
+                        + " ".join(_CFLAGS).encode()
                         + os.uname().machine.encode()).hexdigest()
     if not force and _LIB.exists() and stamp.exists() and stamp.read_text() == fp:
         return _LIB
@@ -77,6 +81,9 @@ def _l():
         lib.orc_decode_param16.argtypes = [fp_, g]
         lib.orc_decode_param16.restype = ctypes.c_int
         lib.orc_set_texture_emulation.argtypes = [ctypes.c_int]
+        lib.orc_tex_fetch1d.argtypes = [fp_, ctypes.c_int, fp_, fp_, ctypes.c_int]
+        lib.orc_tex_fetch2d.argtypes = [fp_, ctypes.c_int, ctypes.c_int, fp_, fp_, fp_,
+                                        ctypes.c_int]
         lib.orc_ray_table.argtypes = [g, fp_, dp, ip]
         lib.orc_fp_fan.argtypes = [g, fp_, dp, dp, ctypes.c_int]
         lib.orc_fp_fan_adjoint.argtypes = [g, fp_, dp, dp, ctypes.c_int]
@@ -135,6 +142,26 @@ def decode(param16) -> OrcGeom:
 
 def set_texture_emulation(on: bool) -> None:
     _l().orc_set_texture_emulation(1 if on else 0)
+
+
+def texture_fetch1d(table, x) -> np.ndarray:
+    """The GPU texture unit's linear filter (texture_rule.h) on a 1-D fp32 row."""
+    t = np.ascontiguousarray(table, np.float32)
+    xs = np.ascontiguousarray(x, np.float32)
+    out = np.empty(xs.size, np.float32)
+    _l().orc_tex_fetch1d(_fptr(t), t.size, _fptr(xs), _fptr(out), xs.size)
+    return out
+
+
+def texture_fetch2d(table, x, y) -> np.ndarray:
+    """The GPU texture unit's linear filter on an h-by-w fp32 image (row = y)."""
+    t = np.ascontiguousarray(table, np.float32)
+    xs = np.ascontiguousarray(x, np.float32)
+    ys = np.ascontiguousarray(y, np.float32)
+    out = np.empty(xs.size, np.float32)
+    _l().orc_tex_fetch2d(_fptr(t), t.shape[1], t.shape[0], _fptr(xs), _fptr(ys), _fptr(out),
+                         xs.size)
+    return out
 
 
 def ray_table(g: OrcGeom, angles):
@@ -350,3 +377,50 @@ def fdk_cone_adjoint(g, n_rows, nz, angles, vol, window: int = RAMLAK, short_sca
                      cosine: bool = False, source_z=None) -> np.ndarray:
     t = ramp_filter(g, cone_bp_transpose(g, n_rows, nz, angles, vol, source_z), window)
     return _weighted(g, angles, t, short_scan, cosine, n_rows, True)
+
+
+# ---- the GPU texture probe (tests/golden/texture_probe.cu) -------------------
+
+_PROBE_SRC = Path(__file__).resolve().parent.parent / "tests" / "golden" / "texture_probe.cu"
+_PROBE_LIB = _BUILD / "libtexprobe.so"
+_probe = None
+
+
+def texture_probe_build(force: bool = False) -> Path:
+    """Compiles the texture probe with nvcc for sm_103a (needs the CUDA toolkit)."""
+    _BUILD.mkdir(parents=True, exist_ok=True)
+    stamp = _BUILD / "texprobe.stamp"
+    fp = hashlib.sha256(_PROBE_SRC.read_bytes() + os.uname().machine.encode()).hexdigest()
+    if not force and _PROBE_LIB.exists() and stamp.exists() and stamp.read_text() == fp:
+        return _PROBE_LIB
+    tmp = _BUILD / "libtexprobe.so.tmp"
+    cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-shared",
+           "-Xcompiler", "-fPIC", str(_PROBE_SRC), "-o", str(tmp)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"texture probe build failed: {' '.join(cmd)}\n{res.stderr}")
+    os.replace(tmp, _PROBE_LIB)
+    stamp.write_text(fp)
+    return _PROBE_LIB
+
+
+def texture_probe_fetch(table, x, y=None) -> np.ndarray:
+    """Fetches through a real texture object on the current GPU: a 1-D row
+    when ``y`` is None, else an h-by-w image (row = y)."""
+    global _probe
+    if _probe is None:
+        lib = ctypes.CDLL(str(texture_probe_build()))
+        fp_ = ctypes.POINTER(ctypes.c_float)
+        lib.texprobe_fetch.argtypes = [fp_, ctypes.c_int, ctypes.c_int, fp_, fp_, fp_,
+                                       ctypes.c_int]
+        lib.texprobe_fetch.restype = ctypes.c_int
+        _probe = lib
+    t = np.ascontiguousarray(table, np.float32)
+    xs = np.ascontiguousarray(x, np.float32)
+    ys = xs if y is None else np.ascontiguousarray(y, np.float32)
+    w, h = (t.size, 0) if y is None else (t.shape[1], t.shape[0])
+    out = np.empty(xs.size, np.float32)
+    rc = _probe.texprobe_fetch(_fptr(t), w, h, _fptr(xs), _fptr(ys), _fptr(out), xs.size)
+    if rc != 0:
+        raise RuntimeError(f"texture probe failed with CUDA error {rc}")
+    return out

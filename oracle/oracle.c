@@ -4,28 +4,33 @@
  * the CPU-baseline leg of the benchmark call it as the checker; no product
  * code path links or executes it.
  *
- * Parity status: UNPINNED against the reference's own outputs.  The reference
- * cannot be built here (legacy texture references do not compile with CUDA 13;
- * TensorFlow, Intel IPP and helper_cuda.h are absent) and ships no tests,
- * golden vectors or fixtures (its only input, test.fbp, is missing).  What
- * pins this restatement instead: the reference's own Python geometry packing
- * (utils.py, config.py) executed to produce golden parameter/angle vectors,
- * exact known answers of the discrete operators (constant image, constant
- * sinogram), analytic ellipse line integrals, and FP64 adjoint identities.
+ * Parity status: PINNED to the reference's own ops, executed.  The reference
+ * cannot be built for the GPU here (legacy texture references do not compile
+ * with CUDA 13; TensorFlow, Intel IPP and helper_cuda.h are absent), so its op
+ * wrappers and CUDA sources are compiled for the host against stand-ins for
+ * those three (build_ref.py, refexec/) and executed; the outputs are the
+ * golden vectors of tests/golden/reference_ops.npz.  With the texture unit's
+ * weights (texture_rule.h) this restatement meets them within 2e-6 (FP),
+ * 1e-6 (BP) and 5e-5 (FBP, FDK) relative L2.  Further pins: the reference's
+ * Python geometry packing (utils.py, config.py) executed for golden
+ * parameter/angle vectors, exact known answers of the discrete operators,
+ * analytic ellipse line integrals, and FP64 adjoint identities.
  *
  * Every function follows the reference's arithmetic in double precision,
  * citing the file:line it restates.  Geometry decoding stays in float, as the
  * op constructors do it, because those floats are the op's attributes.
  *
- * Optional texture emulation (orc_set_texture_emulation(1)) quantises the
- * linear-filter fractions to 8 fractional bits, the documented precision of
- * CUDA's hardware texture filtering, to bound how far the reference's
- * texture-unit outputs sit from exact bilinear interpolation.
+ * Optional texture emulation (orc_set_texture_emulation(1)) applies the GPU
+ * texture unit's linear-filter weights (texture_rule.h: fractions rounded to
+ * 1/256, the 2-D far-corner weight rounded to 1/256) to bound how far the
+ * reference's texture-unit outputs sit from exact bilinear interpolation.
  */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include "texture_rule.h"
 
 #define ORC_PI_F 3.14159265359f /* FP/transform.h:1 */
 #define ORC_STEP 0.125          /* FP/transform.cu:10 */
@@ -143,7 +148,8 @@ void orc_ray_table(const orc_geom *g, const float *angles, double *ray, int32_t 
 }
 
 /* tex2D with cudaFilterModeLinear + cudaAddressModeClamp on an nx-by-ny float
- * array: texel (i, j) centred at (i+1/2, j+1/2), clamp-to-edge taps. */
+ * array: texel (i, j) centred at (i+1/2, j+1/2), clamp-to-edge taps.  With
+ * texture emulation on, the weights are the texture unit's (texture_rule.h). */
 typedef struct tap4 {
     int i0, i1, j0, j1;
     double w00, w10, w01, w11;
@@ -159,11 +165,30 @@ static tap4 bilinear_taps(int nx, int ny, double x, double y) {
     t.i1 = i + 1 < 0 ? 0 : (i + 1 > nx - 1 ? nx - 1 : i + 1);
     t.j0 = j < 0 ? 0 : (j > ny - 1 ? ny - 1 : j);
     t.j1 = j + 1 < 0 ? 0 : (j + 1 > ny - 1 ? ny - 1 : j + 1);
+    if (g_tex8) {
+        int k[4];
+        ctex_weights2d((int)(ax * 256.0), (int)(ay * 256.0), k);
+        t.w00 = k[0] / 256.0;
+        t.w10 = k[1] / 256.0;
+        t.w01 = k[2] / 256.0;
+        t.w11 = k[3] / 256.0;
+        return t;
+    }
     t.w00 = (1.0 - ax) * (1.0 - ay);
     t.w10 = ax * (1.0 - ay);
     t.w01 = (1.0 - ax) * ay;
     t.w11 = ax * ay;
     return t;
+}
+
+/* The texture unit's filter (texture_rule.h) on n coordinates, so that the
+ * tests can hold the rule against fetches measured on the GPU. */
+void orc_tex_fetch1d(const float *t, int w, const float *x, float *out, int n) {
+    for (int k = 0; k < n; ++k) out[k] = ctex_fetch1d(t, w, x[k]);
+}
+void orc_tex_fetch2d(const float *t, int w, int h, const float *x, const float *y, float *out,
+                     int n) {
+    for (int k = 0; k < n; ++k) out[k] = ctex_fetch2d(t, w, h, x[k], y[k]);
 }
 
 /* RayTrace_ReconImage_OneView_kernel, FP/transform.cu:103-146:
