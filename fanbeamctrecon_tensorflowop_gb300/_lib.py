@@ -83,7 +83,7 @@ class CtBatchConfig(ctypes.Structure):
 class CtPlanOpts(ctypes.Structure):
     _fields_ = [("filter_window", ctypes.c_int32), ("filter_algo", ctypes.c_int32),
                 ("short_scan", ctypes.c_int32), ("cosine_weight", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("texture_weights", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 _vp = ctypes.c_void_p

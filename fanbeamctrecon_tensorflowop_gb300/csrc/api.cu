@@ -217,6 +217,7 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
             if (r != 0) return CT_ERR_INVALID_ARGUMENT;
         if (o.short_scan != 0 && o.short_scan != 1) return CT_ERR_INVALID_ARGUMENT;
         if (o.cosine_weight != 0 && o.cosine_weight != 1) return CT_ERR_INVALID_ARGUMENT;
+        if (o.texture_weights != 0 && o.texture_weights != 1) return CT_ERR_INVALID_ARGUMENT;
     }
     if (o.filter_window != CT_WINDOW_RAMLAK && o.filter_window != CT_WINDOW_SHEPP_LOGAN)
         return CT_ERR_INVALID_ARGUMENT;
@@ -651,6 +652,7 @@ ct_status ct_plain_bp_fan(const ct_plan *plan, const float *d_sino, float *d_img
                           ct_stream stream) {
     ct_status st = check_call(plan, d_sino, d_img, batch);
     if (st != CT_OK || batch == 0) return st;
+    if (plan->opts.texture_weights) return CT_ERR_UNSUPPORTED;  // the loop keeps exact weights
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
     return launch_status(ctk::plain_bp_fan(plan, d_sino, d_img, batch, stream), "ct_plain_bp_fan");

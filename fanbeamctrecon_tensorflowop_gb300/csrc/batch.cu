@@ -288,6 +288,8 @@ ct_status check_items(const ct_batch_item *items, int n) {
             return CT_ERR_INVALID_ARGUMENT;
         if (it.d_in == it.d_out) return CT_ERR_INVALID_ARGUMENT;
         if (it.plan->device != items[0].plan->device) return CT_ERR_INVALID_ARGUMENT;
+        // the persistent backprojection keeps exact weights only
+        if (it.op != CT_OP_FP && it.plan->opts.texture_weights) return CT_ERR_UNSUPPORTED;
         if ((it.op == CT_OP_FBP || it.op == CT_OP_FBP_ADJOINT) &&
             it.plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
             ramp_direct_smem(it.plan->g.n_cols) > 227 * 1024)

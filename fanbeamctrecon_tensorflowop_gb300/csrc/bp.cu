@@ -15,6 +15,8 @@
 // for up to four slices.  t/U uses the SFU reciprocal; atan(z) is a
 // polynomial in z^2 fitted per plan over the FOV's |z| range (to FP32 atanf
 // accuracy, 3e-8 absolute), with atanf kept for fans wider than 90 degrees.
+// Plans with texture_weights = 1 round the interpolation weight as the
+// reference's texture unit does (tex_weight); the default keeps exact FP32.
 #include "bp_body.cuh"
 
 namespace ctk {
@@ -24,14 +26,16 @@ constexpr int kTile = kBpTile;
 constexpr int kBptSlices = 4;  // slices per transpose thread (measured: 1 -> 16.2 ms, 4 -> 15.5, 8 -> 17.2)
 constexpr int kRowsPerThr = kBpRowsPerThr;
 
-template <bool WEIGHTED, int SB, int DEG>
+template <bool WEIGHTED, int SB, int DEG, bool TEX>
 __global__ void __launch_bounds__(256)
     bp_fan_kernel(const float *__restrict__ sino, float *__restrict__ img,
                   const float2 *__restrict__ view_cs, BpArgs a, int batch) {
     const int b0 = blockIdx.z * SB;
     const size_t slice = (size_t)a.V * a.C, plane = (size_t)a.nx * a.ny;
-    bp_tile<WEIGHTED, SB, DEG, float>(sino + b0 * slice, slice, img + b0 * plane, plane, view_cs,
-                                      a, min(SB, batch - b0), blockIdx.x, blockIdx.y);
+    bp_tile<WEIGHTED, SB, DEG, float, kBpRowsPerThr, TEX>(sino + b0 * slice, slice,
+                                                          img + b0 * plane, plane, view_cs, a,
+                                                          min(SB, batch - b0), blockIdx.x,
+                                                          blockIdx.y);
 }
 
 // Transpose of bp_fan_kernel: each pixel-view scatters x * weight * (1-f, f)
@@ -39,7 +43,7 @@ __global__ void __launch_bounds__(256)
 // thread evaluates each pixel-view's geometry once for GSB slices.  (A
 // shared-memory, fixed-point form with one block per view measured slower:
 // every block then sweeps the whole image.)
-template <bool WEIGHTED, int DEG, int GSB>
+template <bool WEIGHTED, int DEG, int GSB, bool TEX>
 __global__ void __launch_bounds__(256)
     bp_fan_transpose_kernel(const float *__restrict__ img, float *__restrict__ sino,
                             const float2 *__restrict__ view_cs, BpArgs a, int batch) {
@@ -84,6 +88,7 @@ __global__ void __launch_bounds__(256)
                 int i;
                 float f;
                 split_pos(y, i, f);
+                if constexpr (TEX) f = tex_weight(f);
                 const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
                 const float w = WEIGHTED ? __fdividef(1.0f, fmaf(U, U, t * t)) : 1.0f;
 #pragma unroll
@@ -119,28 +124,39 @@ BpArgs make_args(const ct_plan *p) {
     return a;
 }
 
-template <bool W, int SB>
+template <bool W, int SB, bool TEX>
 void launch_bp(int deg, dim3 grid, cudaStream_t s, const float *sp, float *ip, const float2 *vcs,
                const BpArgs &a, int nb) {
     dim3 block(kTile, 8, 1);
     if (deg == 4)
-        bp_fan_kernel<W, SB, 4><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
+        bp_fan_kernel<W, SB, 4, TEX><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
     else if (deg == 8)
-        bp_fan_kernel<W, SB, 8><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
+        bp_fan_kernel<W, SB, 8, TEX><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
     else
-        bp_fan_kernel<W, SB, 0><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
+        bp_fan_kernel<W, SB, 0, TEX><<<grid, block, 0, s>>>(sp, ip, vcs, a, nb);
 }
 
-template <bool W>
+template <int SB>
+void launch_bp_any(bool w, bool tex, int deg, dim3 grid, cudaStream_t s, const float *sp,
+                   float *ip, const float2 *vcs, const BpArgs &a, int nb) {
+    if (w)
+        (tex ? launch_bp<true, SB, true> : launch_bp<true, SB, false>)(deg, grid, s, sp, ip, vcs,
+                                                                      a, nb);
+    else
+        (tex ? launch_bp<false, SB, true> : launch_bp<false, SB, false>)(deg, grid, s, sp, ip,
+                                                                        vcs, a, nb);
+}
+
+template <bool W, bool TEX>
 void launch_bpt(int deg, dim3 grid, cudaStream_t s, const float *ip, float *sp, const float2 *vcs,
                 const BpArgs &a, int nb) {
     dim3 block(kTile, 8, 1);
     if (deg == 4)
-        bp_fan_transpose_kernel<W, 4, kBptSlices><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+        bp_fan_transpose_kernel<W, 4, kBptSlices, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
     else if (deg == 8)
-        bp_fan_transpose_kernel<W, 8, kBptSlices><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+        bp_fan_transpose_kernel<W, 8, kBptSlices, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
     else
-        bp_fan_transpose_kernel<W, 0, kBptSlices><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+        bp_fan_transpose_kernel<W, 0, kBptSlices, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
 }
 
 }  // namespace
@@ -157,17 +173,11 @@ int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weigh
         dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + kTile - 1) / kTile, (nb + SB - 1) / SB);
         const float *sp = sino + (size_t)b0 * a.V * a.C;
         float *ip = img + (size_t)b0 * a.nx * a.ny;
-        if (SB == 4) {
-            if (weighted)
-                launch_bp<true, 4>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
-            else
-                launch_bp<false, 4>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
-        } else {
-            if (weighted)
-                launch_bp<true, 1>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
-            else
-                launch_bp<false, 1>(p->atan_deg, grid, s, sp, ip, vcs, a, nb);
-        }
+        const bool tex = p->opts.texture_weights != 0;
+        if (SB == 4)
+            launch_bp_any<4>(weighted != 0, tex, p->atan_deg, grid, s, sp, ip, vcs, a, nb);
+        else
+            launch_bp_any<1>(weighted != 0, tex, p->atan_deg, grid, s, sp, ip, vcs, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();
@@ -186,10 +196,13 @@ int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch,
         dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + kTile - 1) / kTile, (nb + G - 1) / G);
         const float *ip = img + (size_t)b0 * a.nx * a.ny;
         float *sp = sino + (size_t)b0 * a.V * a.C;
+        const bool tex = p->opts.texture_weights != 0;
         if (weighted)
-            launch_bpt<true>(p->atan_deg, grid, s, ip, sp, vcs, a, nb);
+            (tex ? launch_bpt<true, true> : launch_bpt<true, false>)(p->atan_deg, grid, s, ip, sp,
+                                                                    vcs, a, nb);
         else
-            launch_bpt<false>(p->atan_deg, grid, s, ip, sp, vcs, a, nb);
+            (tex ? launch_bpt<false, true> : launch_bpt<false, false>)(p->atan_deg, grid, s, ip,
+                                                                      sp, vcs, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();

@@ -41,11 +41,24 @@ __device__ __forceinline__ void split_pos(float y, int &i, float &f) {
     f = y - (m - 12582912.0f);
 }
 
+// The GPU texture unit's linear-filter weight for a fraction f in [0, 1): f
+// rounded to a multiple of 1/256, ties up (8 fractional bits; measured on
+// GB300 against texture objects with the reference's sampler state).  The
+// reference interpolates its sinogram rows through the texture unit
+// (BP/transform.cu:90, FBP/transform.cu:85, FDK/GPURecon_GPU.cu:45); plans
+// created with texture_weights = 1 reproduce it.  f * 256 + 1/2 is exact in
+// FP32, so this is the rounding itself, not an approximation of it.
+__device__ __forceinline__ float tex_weight(float f) {
+    return floorf(fmaf(f, 256.0f, 0.5f)) * (1.0f / 256.0f);
+}
+
 // One 32 x (8 ROWS) tile (tx, ty) of nsl <= SB slices: sino slice s at
 // sino + s * sstride ([V][C]), image slice s at img + s * istride ([ny][nx]).
 // Block of 32 x 8 threads, ROWS pixels per thread (32 x 32 tiles by default);
-// block-uniform call.
-template <bool WEIGHTED, int SB, int DEG, typename OutT, int ROWS = kBpRowsPerThr>
+// block-uniform call.  TEX: texture-unit weights (tex_weight) instead of
+// exact FP32 ones.
+template <bool WEIGHTED, int SB, int DEG, typename OutT, int ROWS = kBpRowsPerThr,
+          bool TEX = false>
 __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t sstride,
                                         OutT *__restrict__ img, size_t istride,
                                         const float2 *__restrict__ view_cs, const BpArgs &a,
@@ -88,6 +101,7 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
                     int i;
                     float f;
                     split_pos(y, i, f);
+                    if constexpr (TEX) f = tex_weight(f);
                     const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
                     float wgt = 1.0f;
                     if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));

@@ -57,12 +57,22 @@ __device__ __forceinline__ void split_pos(float y, int &i, float &f) {
     f = y - (m - 12582912.0f);
 }
 
+// The texture unit's 2-D weights (tex2D with linear filtering, the reference's
+// FDK/GPURecon_GPU.cu:45): A, B = the column and row fractions in 1/256
+// (tex_weight * 256); the far corner gets round(A B / 256) and the other
+// three complete exact row and column sums (measured on GB300).  Returns
+// w00 (r0, i0), w01 (r0, i1), w10 (r1, i0), w11 (r1, i1), in units of 1/256.
+__device__ __forceinline__ float4 tex_weights2d(float A, float B) {
+    const float w11 = floorf(fmaf(A, B, 128.0f) * (1.0f / 256.0f));
+    return make_float4(256.0f - A - B + w11, A - w11, B - w11, w11);
+}
+
 // ---- CB_EA backprojection ----------------------------------------------------
 // Thread = one (x, y) pixel and ZC consecutive z slices; block = 32 x 8 pixels.
 // Per view the column, the 1/(U^2+t^2) weight and the row slope are computed
 // once; each slice then needs one row coordinate and a bilinear (col, row)
 // sample of the view (FDK/GPURecon_GPU.cu:33-47).
-template <int ZC, int DEG>
+template <int ZC, int DEG, bool TEX>
 __global__ void __launch_bounds__(kThreads)
     cone_bp_kernel(const float *__restrict__ proj, float *__restrict__ vol,
                    const float2 *__restrict__ view_cs, const float *__restrict__ view_z,
@@ -94,6 +104,7 @@ __global__ void __launch_bounds__(kThreads)
             int ic;
             float f;
             split_pos(y, ic, f);
+            const float A = floorf(fmaf(f, 256.0f, 0.5f));  // used with TEX only
             const int i0 = max(ic - 1, 0), i1 = min(ic, a.C - 1);
             const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
             const float *pv = pb + (size_t)v * pview;
@@ -114,8 +125,14 @@ __global__ void __launch_bounds__(kThreads)
                 const float *ra = pv + (size_t)r0 * a.C, *rc = pv + (size_t)r1 * a.C;
                 const float va0 = __ldg(ra + i0), va1 = __ldg(ra + i1);
                 const float vc0 = __ldg(rc + i0), vc1 = __ldg(rc + i1);
-                const float lo = fmaf(f, va1 - va0, va0), hi = fmaf(f, vc1 - vc0, vc0);
-                acc[kk] = fmaf(fmaf(fr, hi - lo, lo), wgt, acc[kk]);
+                if constexpr (TEX) {
+                    const float4 w = tex_weights2d(A, floorf(fmaf(fr, 256.0f, 0.5f)));
+                    const float val = fmaf(w.x, va0, fmaf(w.y, va1, fmaf(w.z, vc0, w.w * vc1)));
+                    acc[kk] = fmaf(val * (1.0f / 256.0f), wgt, acc[kk]);
+                } else {
+                    const float lo = fmaf(f, va1 - va0, va0), hi = fmaf(f, vc1 - vc0, vc0);
+                    acc[kk] = fmaf(fmaf(fr, hi - lo, lo), wgt, acc[kk]);
+                }
             }
         }
     }
@@ -148,7 +165,7 @@ constexpr int kRB = 16;
 #define CT_CONE_T_TILES 1
 #endif
 
-template <int DEG>
+template <int DEG, bool TEX>
 __global__ void __launch_bounds__(kThreads)
     cone_bp_transpose_kernel(const float *__restrict__ vol, float *__restrict__ proj,
                              const float2 *__restrict__ view_cs, const float *__restrict__ view_z,
@@ -198,6 +215,8 @@ __global__ void __launch_bounds__(kThreads)
         int ic;
         float f;
         split_pos(y, ic, f);
+        const float A = floorf(fmaf(f, 256.0f, 0.5f));  // used with TEX only
+        if constexpr (TEX) f = A * (1.0f / 256.0f);
         const int i0 = max(ic - 1, 0), i1 = min(ic, a.C - 1);
         const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
         const float slope = a.row_scale * rU;
@@ -234,13 +253,26 @@ __global__ void __launch_bounds__(kThreads)
                 continue;
             }
             const float vs = val * scale;
+            float w00, w01, w10, w11;  // (r0, i0), (r0, i1), (r1, i0), (r1, i1)
+            if constexpr (TEX) {
+                const float4 w = tex_weights2d(A, floorf(fmaf(fr, 256.0f, 0.5f)));
+                w00 = w.x * (1.0f / 256.0f);
+                w01 = w.y * (1.0f / 256.0f);
+                w10 = w.z * (1.0f / 256.0f);
+                w11 = w.w * (1.0f / 256.0f);
+            } else {
+                w00 = (1.0f - fr) * (1.0f - f);
+                w01 = (1.0f - fr) * f;
+                w10 = fr * (1.0f - f);
+                w11 = fr * f;
+            }
             if ((unsigned)r0 < (unsigned)nr) {
-                atomicAdd(&rows_acc[r0 * a.C + i0], __float2int_rn(vs * (1.0f - fr) * (1.0f - f)));
-                atomicAdd(&rows_acc[r0 * a.C + i1], __float2int_rn(vs * (1.0f - fr) * f));
+                atomicAdd(&rows_acc[r0 * a.C + i0], __float2int_rn(vs * w00));
+                atomicAdd(&rows_acc[r0 * a.C + i1], __float2int_rn(vs * w01));
             }
             if ((unsigned)r1 < (unsigned)nr) {
-                atomicAdd(&rows_acc[r1 * a.C + i0], __float2int_rn(vs * fr * (1.0f - f)));
-                atomicAdd(&rows_acc[r1 * a.C + i1], __float2int_rn(vs * fr * f));
+                atomicAdd(&rows_acc[r1 * a.C + i0], __float2int_rn(vs * w10));
+                atomicAdd(&rows_acc[r1 * a.C + i1], __float2int_rn(vs * w11));
             }
         }
     }
@@ -543,12 +575,11 @@ int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *st
         const float *pp = proj + (size_t)b0 * a.V * a.n_rows * a.C;
         float *vp = vol + (size_t)b0 * a.nz * a.ny * a.nx;
         cudaStream_t s = (cudaStream_t)stream;
-        if (a.atan_deg == 4)
-            cone_bp_kernel<ZC, 4><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
-        else if (a.atan_deg == 8)
-            cone_bp_kernel<ZC, 8><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
-        else
-            cone_bp_kernel<ZC, 0><<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
+        const bool tex = p->opts.texture_weights != 0;
+        auto kern = a.atan_deg == 4   ? (tex ? cone_bp_kernel<ZC, 4, true> : cone_bp_kernel<ZC, 4, false>)
+                    : a.atan_deg == 8 ? (tex ? cone_bp_kernel<ZC, 8, true> : cone_bp_kernel<ZC, 8, false>)
+                                      : (tex ? cone_bp_kernel<ZC, 0, true> : cone_bp_kernel<ZC, 0, false>);
+        kern<<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();
@@ -584,9 +615,12 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
     ct_count_launch();
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
     const size_t smem = sizeof(int) * (kRB + 2) * a.C;
-    auto kern = a.atan_deg == 4   ? cone_bp_transpose_kernel<4>
-                : a.atan_deg == 8 ? cone_bp_transpose_kernel<8>
-                                  : cone_bp_transpose_kernel<0>;
+    const bool tex = p->opts.texture_weights != 0;
+    auto kern = a.atan_deg == 4
+                    ? (tex ? cone_bp_transpose_kernel<4, true> : cone_bp_transpose_kernel<4, false>)
+                : a.atan_deg == 8
+                    ? (tex ? cone_bp_transpose_kernel<8, true> : cone_bp_transpose_kernel<8, false>)
+                    : (tex ? cone_bp_transpose_kernel<0, true> : cone_bp_transpose_kernel<0, false>);
     cudaError_t e =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;

@@ -26,14 +26,19 @@ def _ptr(t: torch.Tensor | None) -> int | None:
 
 
 class FanPlan:
-    """A fan-beam geometry bound to one CUDA device."""
+    """A fan-beam geometry bound to one CUDA device.
+
+    ``texture_weights=True`` makes the backprojectors (BP, FBP, the FDK op and
+    their adjoints) interpolate with the GPU texture unit's 8-bit weights, as
+    the reference's texture fetches did; the default interpolates with exact
+    FP32 weights.  The forward projector is exact either way."""
 
     n_rows = 1
     nz = 1
 
     def __init__(self, param16, angles, device=None, window: int = _lib.WINDOW_RAMLAK,
                  filter_algo: int = _lib.FILTER_AUTO, short_scan: bool = False,
-                 cosine_weight: bool = False):
+                 cosine_weight: bool = False, texture_weights: bool = False):
         self._lib = _lib.load()
         self.param16 = np.ascontiguousarray(np.asarray(param16, dtype=np.float32)).copy()
         self.angles = np.ascontiguousarray(np.asarray(angles, dtype=np.float32)).copy()
@@ -41,6 +46,7 @@ class FanPlan:
         self.window = int(window)
         self.short_scan = bool(short_scan)
         self.cosine_weight = bool(cosine_weight)
+        self.texture_weights = bool(texture_weights)
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device)
@@ -51,6 +57,7 @@ class FanPlan:
         opts.filter_algo = int(filter_algo)
         opts.short_scan = int(self.short_scan)
         opts.cosine_weight = int(self.cosine_weight)
+        opts.texture_weights = int(self.texture_weights)
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             st = self._create(opts, handle)
@@ -207,13 +214,13 @@ class ConePlan(FanPlan):
 
     def __init__(self, param16, angles, n_rows: int, nz: int, device=None,
                  window: int = _lib.WINDOW_RAMLAK, short_scan: bool = False,
-                 cosine_weight: bool = False, source_z=None):
+                 cosine_weight: bool = False, source_z=None, texture_weights: bool = False):
         self.n_rows = int(n_rows)
         self.nz = int(nz)
         self.source_z = (None if source_z is None else
                          np.ascontiguousarray(np.asarray(source_z, dtype=np.float32)).copy())
         super().__init__(param16, angles, device=device, window=window, short_scan=short_scan,
-                         cosine_weight=cosine_weight)
+                         cosine_weight=cosine_weight, texture_weights=texture_weights)
 
     def _create(self, opts, handle) -> int:
         fptr = ctypes.POINTER(ctypes.c_float)

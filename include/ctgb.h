@@ -118,7 +118,18 @@ typedef struct ct_plan_opts {
      * reference has none (FBP/transform.cu:61-89 weights by 1/L^2 only).
      * 0: no pre-weighting (the reference). */
     int32_t cosine_weight;
-    int32_t reserved[4];    /* must be zero      */
+    /* 1: backprojectors interpolate with the GPU texture unit's weights, as
+     * the reference's tex1D/tex2D did (BP/transform.cu:90,
+     * FBP/transform.cu:85, FDK/GPURecon_GPU.cu:45): each fraction rounded to
+     * 1/256, ties up, and in 2-D the far-corner weight rounded to 1/256 with
+     * the other three completing exact row and column sums.  Applies to BP,
+     * FBP, the FDK ops and their adjoints (which stay exact transposes).
+     * The forward projectors keep exact weights: their cell sums have no
+     * per-sample weight to round.  ct_batch_run and the ct_plain_* loop
+     * reject such plans (CT_ERR_UNSUPPORTED).
+     * 0: exact FP32 weights (default). */
+    int32_t texture_weights;
+    int32_t reserved[3];    /* must be zero      */
 } ct_plan_opts;
 
 /* Operators, for ct_workspace_size. */

@@ -281,6 +281,22 @@ static int bp_col(const orc_geom *g, double x, double y, double c, double s, int
     return 1;
 }
 
+/* Weights of a (column, row) sample whose fractions f, fr came through frac_w:
+ * w[0] (row r0, col i0), w[1] (r0, i1), w[2] (r1, i0), w[3] (r1, i1).  Exact
+ * bilinear, or with texture emulation the texture unit's (texture_rule.h). */
+static void bilinear_w(double f, double fr, double w[4]) {
+    if (g_tex8) {
+        int k[4];
+        ctex_weights2d((int)(f * 256.0), (int)(fr * 256.0), k);
+        for (int n = 0; n < 4; ++n) w[n] = k[n] / 256.0;
+        return;
+    }
+    w[0] = (1.0 - f) * (1.0 - fr);
+    w[1] = f * (1.0 - fr);
+    w[2] = (1.0 - f) * fr;
+    w[3] = f * fr;
+}
+
 /* BackProjOneView_fan_curve_kernel summed over views (BP/transform.cu:67-95,
  * 110-119); weighted != 0 adds the 1/(U^2+t^2) factor of FBP/transform.cu:78. */
 void orc_bp_fan(const orc_geom *g, const float *angles, const double *sino, double *img,
@@ -503,9 +519,11 @@ void orc_fdk_bp(const orc_geom *g, const float *angles, int window, const double
                                     r0 + 1 < 0 ? 0 : (r0 + 1 > n_rows - 1 ? n_rows - 1 : r0 + 1);
                                 const double *va = sb + ((size_t)v * n_rows + ra) * C;
                                 const double *vc = sb + ((size_t)v * n_rows + rc) * C;
-                                const double a = (1.0 - f) * va[i0] + f * va[i1];
-                                const double cval = (1.0 - f) * vc[i0] + f * vc[i1];
-                                acc += ((1.0 - fr) * a + fr * cval) / (U * U + t * t);
+                                double w[4];
+                                bilinear_w(f, fr, w);
+                                acc += (w[0] * va[i0] + w[1] * va[i1] + w[2] * vc[i0] +
+                                        w[3] * vc[i1]) /
+                                       (U * U + t * t);
                             }
                         }
                     }
@@ -566,9 +584,11 @@ static void cone_bp_impl(const orc_geom *g, int n_rows, int nz, const float *ang
                             const int ra = q < 0 ? 0 : (q > n_rows - 1 ? n_rows - 1 : q);
                             const int rc = q + 1 < 0 ? 0 : (q + 1 > n_rows - 1 ? n_rows - 1 : q + 1);
                             const double *va = pv + (size_t)ra * C, *vc = pv + (size_t)rc * C;
-                            const double lo = (1.0 - f) * va[i0] + f * va[i1];
-                            const double hi = (1.0 - f) * vc[i0] + f * vc[i1];
-                            vb[((size_t)k * ny + j) * nx + i] += ((1.0 - fr) * lo + fr * hi) * wgt;
+                            double w[4];
+                            bilinear_w(f, fr, w);
+                            vb[((size_t)k * ny + j) * nx + i] +=
+                                (w[0] * va[i0] + w[1] * va[i1] + w[2] * vc[i0] + w[3] * vc[i1]) *
+                                wgt;
                         }
                     }
                 }
@@ -601,10 +621,12 @@ static void cone_bp_impl(const orc_geom *g, int n_rows, int nz, const float *ang
                             const int ra = q < 0 ? 0 : (q > n_rows - 1 ? n_rows - 1 : q);
                             const int rc = q + 1 < 0 ? 0 : (q + 1 > n_rows - 1 ? n_rows - 1 : q + 1);
                             if (val == 0.0) continue;
-                            pv[(size_t)ra * C + i0] += val * (1.0 - fr) * (1.0 - f);
-                            pv[(size_t)ra * C + i1] += val * (1.0 - fr) * f;
-                            pv[(size_t)rc * C + i0] += val * fr * (1.0 - f);
-                            pv[(size_t)rc * C + i1] += val * fr * f;
+                            double w[4];
+                            bilinear_w(f, fr, w);
+                            pv[(size_t)ra * C + i0] += val * w[0];
+                            pv[(size_t)ra * C + i1] += val * w[1];
+                            pv[(size_t)rc * C + i0] += val * w[2];
+                            pv[(size_t)rc * C + i1] += val * w[3];
                         }
                     }
                 }
