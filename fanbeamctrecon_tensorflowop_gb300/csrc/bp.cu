@@ -23,7 +23,9 @@ namespace ctk {
 namespace {
 
 constexpr int kTile = kBpTile;
-constexpr int kBptSlices = 4;  // slices per transpose thread (measured: 1 -> 16.2 ms, 4 -> 15.5, 8 -> 17.2)
+// slices per transpose thread for batches of 4 or more (32 clinical slices:
+// 1 -> 16.2 ms, 4 -> 15.5, 8 -> 17.2); smaller batches take one per thread
+constexpr int kBptSlices = 4;
 constexpr int kRowsPerThr = kBpRowsPerThr;
 
 template <bool WEIGHTED, int SB, int DEG, bool TEX>
@@ -147,16 +149,27 @@ void launch_bp_any(bool w, bool tex, int deg, dim3 grid, cudaStream_t s, const f
                                                                         vcs, a, nb);
 }
 
-template <bool W, bool TEX>
+template <bool W, int G, bool TEX>
 void launch_bpt(int deg, dim3 grid, cudaStream_t s, const float *ip, float *sp, const float2 *vcs,
                 const BpArgs &a, int nb) {
     dim3 block(kTile, 8, 1);
     if (deg == 4)
-        bp_fan_transpose_kernel<W, 4, kBptSlices, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+        bp_fan_transpose_kernel<W, 4, G, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
     else if (deg == 8)
-        bp_fan_transpose_kernel<W, 8, kBptSlices, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+        bp_fan_transpose_kernel<W, 8, G, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
     else
-        bp_fan_transpose_kernel<W, 0, kBptSlices, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+        bp_fan_transpose_kernel<W, 0, G, TEX><<<grid, block, 0, s>>>(ip, sp, vcs, a, nb);
+}
+
+template <int G>
+void launch_bpt_any(bool w, bool tex, int deg, dim3 grid, cudaStream_t s, const float *ip,
+                    float *sp, const float2 *vcs, const BpArgs &a, int nb) {
+    if (w)
+        (tex ? launch_bpt<true, G, true> : launch_bpt<true, G, false>)(deg, grid, s, ip, sp, vcs,
+                                                                      a, nb);
+    else
+        (tex ? launch_bpt<false, G, true> : launch_bpt<false, G, false>)(deg, grid, s, ip, sp,
+                                                                        vcs, a, nb);
 }
 
 }  // namespace
@@ -190,19 +203,18 @@ int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch,
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemsetAsync(sino, 0, sizeof(float) * (size_t)batch * a.V * a.C, s);
     if (e != cudaSuccess) return (int)e;
-    constexpr int G = kBptSlices;
+    const int G = batch >= kBptSlices ? kBptSlices : 1;
     for (int b0 = 0; b0 < batch; b0 += 65535 * G) {
         const int nb = batch - b0 < 65535 * G ? batch - b0 : 65535 * G;
         dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + kTile - 1) / kTile, (nb + G - 1) / G);
         const float *ip = img + (size_t)b0 * a.nx * a.ny;
         float *sp = sino + (size_t)b0 * a.V * a.C;
         const bool tex = p->opts.texture_weights != 0;
-        if (weighted)
-            (tex ? launch_bpt<true, true> : launch_bpt<true, false>)(p->atan_deg, grid, s, ip, sp,
-                                                                    vcs, a, nb);
+        if (G == kBptSlices)
+            launch_bpt_any<kBptSlices>(weighted != 0, tex, p->atan_deg, grid, s, ip, sp, vcs, a,
+                                       nb);
         else
-            (tex ? launch_bpt<false, true> : launch_bpt<false, false>)(p->atan_deg, grid, s, ip,
-                                                                      sp, vcs, a, nb);
+            launch_bpt_any<1>(weighted != 0, tex, p->atan_deg, grid, s, ip, sp, vcs, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();
