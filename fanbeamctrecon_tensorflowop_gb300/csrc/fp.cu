@@ -17,10 +17,18 @@
 namespace ctk {
 namespace {
 
-constexpr int kFpThreads = 256;
+// A block is one 32-channel group of kFpViews adjacent views (their rays
+// cross nearly the same cells, so the block's warps share L1 lines), and
+// blocks run channel-group-major: the warps resident at any time cover a few
+// channel groups of every view.  Against 8 channel groups of one view per
+// 256-thread block, in view order: 11.04 -> 8.72 ms per 32 clinical slices
+// (2 views per block 8.74, 8 views 8.97, 16 views 9.27; 1 view, channel-major
+// alone 8.87).
+constexpr int kFpViews = 4;
+constexpr int kFpThreads = 32 * kFpViews;
 constexpr int kFpChunk = 64;  // slices per quad-workspace chunk
 #ifndef CT_FP_MIN_BLOCKS
-#define CT_FP_MIN_BLOCKS 2
+#define CT_FP_MIN_BLOCKS 4
 #endif
 #ifndef CT_FP_MAX_SB
 #define CT_FP_MAX_SB 16
@@ -43,8 +51,11 @@ __global__ void __launch_bounds__(kFpThreads, CT_FP_MIN_BLOCKS)
     fp_fan_kernel(const float4 *__restrict__ quads, float *__restrict__ sino,
                   const float4 *__restrict__ ray, const int *__restrict__ nsamp, int V, int C,
                   int wpv, int nx, float w, int batch, int max_iter) {
-    const int gw = blockIdx.x * (kFpThreads / 32) + (threadIdx.x >> 5);
-    if (gw >= V * wpv) return;  // warp-uniform
+    const int nvg = (V + kFpViews - 1) / kFpViews;
+    const int cgroup = blockIdx.x / nvg, vgroup = blockIdx.x - cgroup * nvg;
+    const int v = vgroup * kFpViews + (threadIdx.x >> 5);
+    if (v >= V) return;  // warp-uniform
+    const int gw = v * wpv + cgroup;
     const int b0 = blockIdx.y * SB;
     const size_t lsz = (size_t)(nx + 1) * (nx + 1);
     // slices beyond the batch read slice b0's quads (results dropped)
@@ -72,7 +83,7 @@ int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *wor
     float4 *quads = static_cast<float4 *>(work);
     cudaStream_t s = (cudaStream_t)stream;
     const int wpv = (C + 31) / 32;
-    const int blocks = (V * wpv + kFpThreads / 32 - 1) / (kFpThreads / 32);
+    const int blocks = (V + kFpViews - 1) / kFpViews * wpv;
     const int Q = nx + 1;
     // chunks of at most kFpChunk slices share the quad workspace
     for (int c0 = 0; c0 < batch; c0 += kFpChunk) {
