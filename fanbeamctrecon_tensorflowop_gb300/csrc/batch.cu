@@ -130,7 +130,10 @@ __global__ void __launch_bounds__(256)
     for (int gw = next_warp_unit<DYN>(ctr, -1, first, step); gw < P.total;
          gw = next_warp_unit<DYN>(ctr, gw, first, step)) {
         const FpItem &it = P.it[find_item(P.it, P.n, gw)];  // warp-uniform
-        const int unit = gw - it.unit0;
+        // channel-group-major within the item: consecutive units are adjacent
+        // views of one channel group, whose rays cross the same cells
+        const int u = gw - it.unit0, cg = u / it.V;
+        const int unit = (u - cg * it.V) * it.wpv + cg;
         if (it.out_bf16)
             fp_warp<1, __nv_bfloat16>(it.quads, 0, static_cast<__nv_bfloat16 *>(it.out), 0,
                                       it.ray, it.nsamp, it.V, it.C, it.wpv, it.nx, it.w, 1,
