@@ -13,7 +13,10 @@ sinograms), Shepp-Logan FBP time, and the batch-32 FP + adjoint step against
 the plain per-view launch loop on the same GPU.
 
 ``--impl reference`` times the reference algorithm on the host CPU (the FP64
-oracle restatement, all cores; the reference itself cannot be built).
+oracle restatement, all cores).  The reference's ops cannot be built for the
+GPU, and their host-compiled form (oracle/build_ref.py, which runs each CUDA
+thread as a fiber) exists only where the reference's sources are and is no
+measure of its speed.
 
 Multi-GPU: ``torchrun --nproc-per-node N bench.py --gpus N``: every rank runs
 its own batch (replicas, no collective on the data path); the step time is
@@ -188,9 +191,9 @@ def run_reference(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded ellipse phantom (numpy default_rng seed 0)",
         "config": {"workload": WORKLOAD, "sample": res["sample"],
-                   "note": "the reference's CUDA/TF ops cannot be built (CUDA 13 rejects "
-                           "texture references; TF/IPP absent): its algorithm runs as the "
-                           "FP64 oracle restatement on the host cores"},
+                   "note": "the reference's CUDA/TF ops cannot be built for the GPU (CUDA 13 "
+                           "rejects texture references; TF/IPP absent): its algorithm runs "
+                           "as the FP64 oracle restatement on the host cores"},
         "cpu_baseline": {"value": v, "unit": "Grays/s", "cores": res["cores"], "kind": "port",
                          "sample": res["sample"]},
         "e2e": {"value": v, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
