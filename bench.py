@@ -406,76 +406,96 @@ def main() -> None:
                 "fdk_gvoxel_views_per_s": 512 * 512 * 64 * VIEWS / t_fdk / 1e6}
         del cvol, cproj, crec, cgrad
 
-    # ---- uneven batch: 48 slices cycling 256^2/492 views/512 ch, 384^2/720/736,
-    #      512^2/984/888 (rFOV 179.2 mm), BF16 storage; FP, FBP and FBP adjoint of all
-    #      48 as three ct_batch_run calls recorded in one CUDA graph ----------------------
-    uneven = None
+    # ---- uneven batches, BF16 storage; FP, FBP and FBP adjoint of all 48 slices as
+    #      three ct_batch_run calls recorded in one CUDA graph:
+    #      (a) 48 slices cycling 256^2/492 views/512 ch, 384^2/720/736, 512^2/984/888
+    #          (rFOV 179.2 mm): three plans of 16 slices each, run as slice groups;
+    #      (b) 48 slices of 48 different geometries: the persistent launches, with
+    #          their launch shapes from the autotuner ----------------------------------
+    uneven = uneven_distinct = None
     if not args.no_uneven:
         from fanbeamctrecon_tensorflowop_gb300.batch import UnevenBatch
         from fanbeamctrecon_tensorflowop_gb300.geometry import angle as _ang
         from fanbeamctrecon_tensorflowop_gb300.geometry import fan_param16 as _f16
-        sizes = [(256, 492, 512), (384, 720, 736), (512, 984, 888)]
-        uplans = []
-        for n_, v_, c_ in sizes:
-            up = _f16(sdd=SDD, sid=SID, n_views=v_, n_cols=c_, n=n_, pixel_mm=358.4 / n_,
-                      dcol_rad=DCOL)
-            uplans.append(FanPlan(up, _ang(v_, 0.0), device=dev))
-        fp_items, fbp_items, adj_items = [], [], []
-        rays = 0
-        for k in range(48):
-            pl = uplans[k % 3]
-            n_ = pl.geom.nx
-            img16 = torch.rand((n_, n_), device=dev, generator=gen).to(torch.bfloat16)
-            sino16 = torch.rand(pl.sino_shape, device=dev, generator=gen).to(torch.bfloat16)
-            fp_items.append((pl, "fp", img16, torch.empty(pl.sino_shape, device=dev,
-                                                          dtype=torch.bfloat16)))
-            fbp_items.append((pl, "fbp", sino16, torch.empty(pl.image_shape, device=dev,
-                                                             dtype=torch.bfloat16)))
-            adj_items.append((pl, "fbp_adjoint", img16, torch.empty(pl.sino_shape, device=dev,
-                                                                    dtype=torch.bfloat16)))
-            rays += pl.geom.n_views * pl.geom.n_cols
-        ubs = [UnevenBatch(fp_items), UnevenBatch(fbp_items), UnevenBatch(adj_items)]
 
-        def graph_ms():
+        def uneven_run(sizes):
+            """sizes: one (n, views, channels) per slice; equal sizes share a plan."""
+            plans = {}
+            for sz in sizes:
+                if sz not in plans:
+                    n_, v_, c_ = sz
+                    up = _f16(sdd=SDD, sid=SID, n_views=v_, n_cols=c_, n=n_,
+                              pixel_mm=358.4 / n_, dcol_rad=DCOL)
+                    plans[sz] = FanPlan(up, _ang(v_, 0.0), device=dev)
+            fp_items, fbp_items, adj_items = [], [], []
+            rays = 0
+            for sz in sizes:
+                pl = plans[sz]
+                n_ = pl.geom.nx
+                img16 = torch.rand((n_, n_), device=dev, generator=gen).to(torch.bfloat16)
+                sino16 = torch.rand(pl.sino_shape, device=dev, generator=gen).to(torch.bfloat16)
+                fp_items.append((pl, "fp", img16, torch.empty(pl.sino_shape, device=dev,
+                                                              dtype=torch.bfloat16)))
+                fbp_items.append((pl, "fbp", sino16, torch.empty(pl.image_shape, device=dev,
+                                                                 dtype=torch.bfloat16)))
+                adj_items.append((pl, "fbp_adjoint", img16,
+                                  torch.empty(pl.sino_shape, device=dev, dtype=torch.bfloat16)))
+                rays += pl.geom.n_views * pl.geom.n_cols
+            ubs = [UnevenBatch(fp_items), UnevenBatch(fbp_items), UnevenBatch(adj_items)]
+
+            def graph_ms():
+                for ub in ubs:
+                    ub.run()
+                torch.cuda.synchronize(dev)
+                graph = torch.cuda.CUDAGraph()
+                cap = torch.cuda.Stream(dev)
+                cap.wait_stream(stream)
+                with torch.cuda.stream(cap):
+                    with torch.cuda.graph(graph, stream=cap):
+                        for ub in ubs:
+                            ub.run()
+                stream.wait_stream(cap)
+                for _ in range(args.warmup):
+                    graph.replay()
+                barrier()
+                n_rep = max(3, args.steps // 3)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(n_rep):
+                    graph.replay()
+                e1.record(stream)
+                barrier()
+                return max_over_ranks(e0.elapsed_time(e1)) / n_rep
+
             for ub in ubs:
-                ub.run()
-            torch.cuda.synchronize(dev)
-            graph = torch.cuda.CUDAGraph()
-            cap = torch.cuda.Stream(dev)
-            cap.wait_stream(stream)
-            with torch.cuda.stream(cap):
-                with torch.cuda.graph(graph, stream=cap):
-                    for ub in ubs:
-                        ub.run()
-            stream.wait_stream(cap)
-            for _ in range(args.warmup):
-                graph.replay()
-            barrier()
-            n_rep = max(3, args.steps // 3)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(n_rep):
-                graph.replay()
-            e1.record(stream)
-            barrier()
-            return max_over_ranks(e0.elapsed_time(e1)) / n_rep
+                ub.set_config(None)
+            g_default = graph_ms()
+            # the autotuner picks both persistent launches' shapes per batch
+            t_tune = time.perf_counter()
+            tuned = [ub.tune(reps=2) for ub in ubs]
+            t_tune = time.perf_counter() - t_tune
+            g_ms = graph_ms()
+            out = {"graph_replay_ms": g_ms, "graph_replay_ms_default_shapes": g_default,
+                   "tuned_shapes": {"fp": tuned[0], "fbp": tuned[1], "fbp_adjoint": tuned[2]},
+                   "tune_seconds": t_tune, "slice_ops_per_replay": 3 * len(sizes),
+                   "fp_rays_per_replay": rays, "plans": len(plans)}
+            del ubs, fp_items, fbp_items, adj_items, plans
+            return out
 
-        for ub in ubs:
-            ub.set_config(None)
-        g_default = graph_ms()
-        # the autotuner picks both persistent launches' shapes per batch
-        t_tune = time.perf_counter()
-        tuned = [ub.tune(reps=2) for ub in ubs]
-        t_tune = time.perf_counter() - t_tune
-        g_ms = graph_ms()
-        uneven = {"workload": "48 slices cycling 256^2/492x512, 384^2/720x736, 512^2/984x888, "
-                              "BF16 storage: FP + FBP + FBP adjoint of every slice, 3 "
-                              "ct_batch_run calls in one CUDA graph",
-                  "graph_replay_ms": g_ms, "graph_replay_ms_default_shapes": g_default,
-                  "tuned_shapes": {"fp": tuned[0], "fbp": tuned[1], "fbp_adjoint": tuned[2]},
-                  "tune_seconds": t_tune,
-                  "slice_ops_per_replay": 144, "fp_rays_per_replay": rays}
-        del ubs, fp_items, fbp_items, adj_items
+        cyc = [(256, 492, 512), (384, 720, 736), (512, 984, 888)]
+        uneven = {"workload": "48 slices cycling 256^2/492x512, 384^2/720x736, 512^2/984x888 "
+                              "(three plans, run as slice groups), BF16 storage: FP + FBP + "
+                              "FBP adjoint of every slice, 3 ct_batch_run calls in one CUDA "
+                              "graph"}
+        uneven.update(uneven_run([cyc[k % 3] for k in range(48)]))
+        # 48 geometries: image 256..512, views 492..962, channels 512..888 (multiples of 8)
+        distinct = [(256 + 16 * (k % 17), 492 + 10 * k, 512 + 8 * k) for k in range(48)]
+        uneven_distinct = {"workload": "48 slices of 48 different geometries (image "
+                                       "256^2..512^2, 492..962 views, 512..888 channels), BF16 "
+                                       "storage: FP + FBP + FBP adjoint, persistent launches, "
+                                       "3 ct_batch_run calls in one CUDA graph"}
+        uneven_distinct.update(uneven_run(distinct))
 
     # ---- e2e through the reference-named entry point with host buffers ---------------
     host_imgs = [imgs[k].cpu().numpy() for k in range(2)]
@@ -527,6 +547,7 @@ def main() -> None:
                 "fp_samples_per_slice": plan.total_samples,
                 "cone": cone,
                 "uneven_bf16": uneven,
+                "uneven_distinct_bf16": uneven_distinct,
             },
         }
         print(json.dumps(line))

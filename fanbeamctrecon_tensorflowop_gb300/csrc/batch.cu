@@ -11,6 +11,11 @@
 //   4. one persistent BP launch: blocks pull (item, 32x32 tile) units of every
 //      BP / FBP item (bp_tile, bp_body.cuh);
 //   5. one launch narrows the FBP-adjoint results that are stored as BF16.
+// Slices that share a plan, an operator and a storage type (a "slice group"
+// of two or more items) take the plan's own multi-slice kernels instead,
+// which walk up to 16 slices at once: their inputs are gathered (and
+// widened) into contiguous workspace, and their results scattered (and
+// narrowed) to the items' buffers.  The persistent launches take the rest.
 // Item descriptors travel as __grid_constant__ kernel parameters, so a call
 // needs no host-to-device copy and can be captured in a CUDA graph.
 //
@@ -72,11 +77,12 @@ struct BpBatch {
     BpItem it[kMax];
 };
 
+enum ConvMode { kWiden = 0, kNarrow = 1, kCopy = 2 };  // BF16 -> F32, F32 -> BF16, F32
 struct ConvItem {
     const void *src;
     void *dst;
     long long count;
-    int to_bf16;
+    int mode;
 };
 struct ConvBatch {
     int n;
@@ -194,12 +200,14 @@ __global__ void __launch_bounds__(256) convert_batch_kernel(const __grid_constan
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < it.count;
          k += stride) {
-        if (it.to_bf16)
+        if (it.mode == kNarrow)
             static_cast<__nv_bfloat16 *>(it.dst)[k] =
                 __float2bfloat16(static_cast<const float *>(it.src)[k]);
-        else
+        else if (it.mode == kWiden)
             static_cast<float *>(it.dst)[k] =
                 __bfloat162float(static_cast<const __nv_bfloat16 *>(it.src)[k]);
+        else
+            static_cast<float *>(it.dst)[k] = static_cast<const float *>(it.src)[k];
     }
 }
 
@@ -226,15 +234,77 @@ BpArgs bp_args(const ct_plan *p) {
 
 size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 
+// Slice groups: the items, in order, of every (plan, op, dtype) that two or
+// more items share; group_of[i] is item i's group or -1.
+constexpr int kGroupMin = 2;
+struct Groups {
+    std::vector<std::vector<int>> members;
+    std::vector<int> group_of;
+};
+Groups slice_groups(const ct_batch_item *items, int n) {
+    Groups G;
+    G.group_of.assign(n, -1);
+    std::vector<std::vector<int>> all;
+    for (int i = 0; i < n; ++i) {
+        int g = -1;
+        for (size_t k = 0; k < all.size() && g < 0; ++k) {
+            const ct_batch_item &f = items[all[k][0]];
+            if (f.plan == items[i].plan && f.op == items[i].op && f.dtype == items[i].dtype)
+                g = (int)k;
+        }
+        if (g < 0) {
+            g = (int)all.size();
+            all.emplace_back();
+        }
+        all[(size_t)g].push_back(i);
+    }
+    for (auto &m : all) {
+        if ((int)m.size() < kGroupMin) continue;
+        for (int i : m) G.group_of[(size_t)i] = (int)G.members.size();
+        G.members.push_back(m);
+    }
+    return G;
+}
+
+// Per-slice element counts of an item's input and output.
+long long in_count(const ct_batch_item &it) {
+    const ct_plan *p = it.plan;
+    return (it.op == CT_OP_FP || it.op == CT_OP_FBP_ADJOINT) ? (long long)p->g.nx * p->g.ny
+                                                            : (long long)p->g.n_views * p->g.n_cols;
+}
+long long out_count(const ct_batch_item &it) {
+    const ct_plan *p = it.plan;
+    return (it.op == CT_OP_FP || it.op == CT_OP_FBP_ADJOINT) ? (long long)p->g.n_views * p->g.n_cols
+                                                            : (long long)p->g.nx * p->g.ny;
+}
+
 struct Layout {
     // byte offsets into the workspace, per item (SIZE_MAX = unused); the
     // first 256 bytes hold the dynamic-schedule counters
     std::vector<size_t> quads, in32, filt, out32, wtd;
+    // per slice group: gathered inputs, results before the scatter, and the
+    // plan path's workspace (all FP32, slices contiguous)
+    std::vector<size_t> g_in, g_out, g_work;
     size_t total = 0;
 };
 constexpr size_t kCounterBytes = 256;
 
-Layout plan_layout(const ct_batch_item *items, int n) {
+// Workspace of a slice group's plan path.
+size_t group_work_bytes(const ct_batch_item &it, int g) {
+    const ct_plan *p = it.plan;
+    const size_t sino = sizeof(float) * (size_t)g * p->g.n_views * p->g.n_cols;
+    switch (it.op) {
+        case CT_OP_FP:
+            return fp_fan_work_bytes(p, g);
+        case CT_OP_FBP:  // filtered (+ pre-weighted) sinograms
+        case CT_OP_FBP_ADJOINT:  // transposed (+ filtered) sinograms
+            return (has_preweight(p) ? 2 : 1) * sino;
+        default:
+            return 0;
+    }
+}
+
+Layout plan_layout(const ct_batch_item *items, int n, const Groups &G) {
     Layout L;
     L.quads.assign(n, SIZE_MAX);
     L.in32.assign(n, SIZE_MAX);
@@ -247,7 +317,15 @@ Layout plan_layout(const ct_batch_item *items, int n) {
         off += align256(bytes);
         return o;
     };
+    for (const auto &m : G.members) {
+        const ct_batch_item &f = items[m[0]];
+        const int g = (int)m.size();
+        L.g_in.push_back(take(sizeof(float) * (size_t)g * in_count(f)));
+        L.g_out.push_back(take(sizeof(float) * (size_t)g * out_count(f)));
+        L.g_work.push_back(take(group_work_bytes(f, g)));
+    }
     for (int i = 0; i < n; ++i) {
+        if (G.group_of[(size_t)i] >= 0) continue;
         const ct_plan *p = items[i].plan;
         const size_t img = sizeof(float) * (size_t)p->g.nx * p->g.ny;
         const size_t sino = sizeof(float) * (size_t)p->g.n_views * p->g.n_cols;
@@ -313,7 +391,7 @@ int sm_count() {
 ct_status batch_workspace(const ct_batch_item *items, int n, size_t *bytes) {
     ct_status st = check_items(items, n);
     if (st != CT_OK) return st;
-    *bytes = plan_layout(items, n).total;
+    *bytes = plan_layout(items, n, slice_groups(items, n)).total;
     return CT_OK;
 }
 
@@ -338,7 +416,9 @@ std::vector<int> order_by_work(const ct_batch_item *items, int n, bool largest_f
 int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
               const ct_batch_config &cfg, void **ev) {
     cudaStream_t s = (cudaStream_t)stream;
-    const Layout L = plan_layout(items, n);
+    const Groups G = slice_groups(items, n);
+    const Layout L = plan_layout(items, n, G);
+    auto grouped = [&](int i) { return G.group_of[(size_t)i] >= 0; };
     uint8_t *ws = static_cast<uint8_t *>(work);
     auto at = [&](size_t off) { return static_cast<void *>(ws + off); };
     const int sms = sm_count();
@@ -349,12 +429,75 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
     if (dyn_any && (e = cudaMemsetAsync(ctr, 0, 2 * sizeof(int), s)) != cudaSuccess) return (int)e;
     cudaEvent_t *evs = reinterpret_cast<cudaEvent_t *>(ev);
 
+    // 0: slice groups: gather (widen), the plan's multi-slice kernels, scatter
+    // (narrow)
+    if (!G.members.empty()) {
+        auto convert = [&](const ConvBatch &CB, long long maxc) {
+            const int bx = (int)((maxc + 255) / 256 < 1024 ? (maxc + 255) / 256 : 1024);
+            convert_batch_kernel<<<dim3(bx, CB.n), 256, 0, s>>>(CB);
+            ct_count_launch();
+            return cudaGetLastError();
+        };
+        ConvBatch gather{}, scatter{};
+        long long max_in = 0, max_out = 0;
+        for (size_t gi = 0; gi < G.members.size(); ++gi) {
+            const auto &m = G.members[gi];
+            const long long ci = in_count(items[m[0]]), co = out_count(items[m[0]]);
+            for (size_t k = 0; k < m.size(); ++k) {
+                const ct_batch_item &it = items[m[k]];
+                const bool bf = it.dtype == CT_DTYPE_BF16;
+                gather.it[gather.n++] =
+                    ConvItem{it.d_in, static_cast<float *>(at(L.g_in[gi])) + (size_t)k * ci, ci,
+                             bf ? kWiden : kCopy};
+                scatter.it[scatter.n++] =
+                    ConvItem{static_cast<float *>(at(L.g_out[gi])) + (size_t)k * co, it.d_out, co,
+                             bf ? kNarrow : kCopy};
+            }
+            max_in = std::max(max_in, ci);
+            max_out = std::max(max_out, co);
+        }
+        if ((e = convert(gather, max_in)) != cudaSuccess) return (int)e;
+        for (size_t gi = 0; gi < G.members.size(); ++gi) {
+            const ct_batch_item &f = items[G.members[gi][0]];
+            const ct_plan *p = f.plan;
+            const int g = (int)G.members[gi].size();
+            const float *in = static_cast<const float *>(at(L.g_in[gi]));
+            float *out = static_cast<float *>(at(L.g_out[gi]));
+            float *wk = static_cast<float *>(at(L.g_work[gi]));
+            const size_t sino = (size_t)g * p->g.n_views * p->g.n_cols;
+            const int rows = g * p->g.n_views;
+            int r = 0;
+            if (f.op == CT_OP_FP) {
+                r = fp_fan(p, in, out, g, wk, s);
+            } else if (f.op == CT_OP_BP) {
+                r = bp_fan(p, in, out, g, 0, s);
+            } else if (f.op == CT_OP_FBP) {  // as ct_fbp_fan
+                const float *src = in;
+                if (has_preweight(p)) {
+                    if ((r = apply_preweight(p, in, wk + sino, g, s)) == 0) src = wk + sino;
+                }
+                if (r == 0) r = ramp_filter(p, src, wk, rows, s);
+                if (r == 0) r = bp_fan(p, wk, out, g, 1, s);
+            } else {  // CT_OP_FBP_ADJOINT, as ct_fbp_fan_adjoint
+                r = bp_fan_transpose(p, in, wk, g, 1, s);
+                if (r == 0 && !has_preweight(p)) {
+                    r = ramp_filter(p, wk, out, rows, s);
+                } else if (r == 0) {
+                    r = ramp_filter(p, wk, wk + sino, rows, s);
+                    if (r == 0) r = apply_preweight(p, wk + sino, out, g, s);
+                }
+            }
+            if (r != 0) return r;
+        }
+        if ((e = convert(scatter, max_out)) != cudaSuccess) return (int)e;
+    }
+
     // 1-2: forward projections
     {
         QuadBatch QB{};
         FpBatch FB{};
         for (int i : order_by_work(items, n, cfg.fp_dynamic != 0, true)) {
-            if (items[i].op != CT_OP_FP) continue;
+            if (items[i].op != CT_OP_FP || grouped(i)) continue;
             const ct_plan *p = items[i].plan;
             const int Q = p->g.nx + 1;
             QuadItem &q = QB.it[QB.n++];
@@ -401,12 +544,12 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
         ConvBatch CB{};
         int maxc = 0;
         for (int i = 0; i < n; ++i) {
-            if (items[i].op == CT_OP_FP || items[i].dtype != CT_DTYPE_BF16) continue;
+            if (items[i].op == CT_OP_FP || items[i].dtype != CT_DTYPE_BF16 || grouped(i)) continue;
             const ct_plan *p = items[i].plan;
             const long long cnt = items[i].op == CT_OP_FBP_ADJOINT
                                       ? (long long)p->g.nx * p->g.ny
                                       : (long long)p->g.n_views * p->g.n_cols;
-            CB.it[CB.n++] = ConvItem{items[i].d_in, at(L.in32[i]), cnt, 0};
+            CB.it[CB.n++] = ConvItem{items[i].d_in, at(L.in32[i]), cnt, kWiden};
             maxc = cnt > maxc ? (int)cnt : maxc;
         }
         if (CB.n > 0) {
@@ -418,6 +561,7 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
     }
     // filters (FBP) and transposes + filters (FBP adjoint), per item
     for (int i = 0; i < n; ++i) {
+        if (grouped(i)) continue;
         const ct_plan *p = items[i].plan;
         const bool bf = items[i].dtype == CT_DTYPE_BF16;
         const float *in32 = bf ? static_cast<const float *>(at(L.in32[i]))
@@ -451,7 +595,7 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
         BpBatch BB{};
         const int tile_h = cfg.bp_tile_rows;
         for (int i : order_by_work(items, n, cfg.bp_dynamic != 0, false)) {
-            if (items[i].op != CT_OP_BP && items[i].op != CT_OP_FBP) continue;
+            if ((items[i].op != CT_OP_BP && items[i].op != CT_OP_FBP) || grouped(i)) continue;
             const ct_plan *p = items[i].plan;
             const bool bf = items[i].dtype == CT_DTYPE_BF16;
             BpItem &b = BB.it[BB.n++];
@@ -495,10 +639,11 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
         ConvBatch CB{};
         int maxc = 0;
         for (int i = 0; i < n; ++i) {
-            if (items[i].op != CT_OP_FBP_ADJOINT || items[i].dtype != CT_DTYPE_BF16) continue;
+            if (items[i].op != CT_OP_FBP_ADJOINT || items[i].dtype != CT_DTYPE_BF16 || grouped(i))
+                continue;
             const ct_plan *p = items[i].plan;
             const long long cnt = (long long)p->g.n_views * p->g.n_cols;
-            CB.it[CB.n++] = ConvItem{at(L.out32[i]), items[i].d_out, cnt, 1};
+            CB.it[CB.n++] = ConvItem{at(L.out32[i]), items[i].d_out, cnt, kNarrow};
             maxc = cnt > maxc ? (int)cnt : maxc;
         }
         if (CB.n > 0) {
@@ -597,8 +742,11 @@ int batch_tune(const ct_batch_item *items, int n, void *work, void *stream, int 
     cudaEvent_t ev[4] = {};
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
+    // only the persistent launches (items outside slice groups) have shapes
     bool has_fp = false, has_bp = false;
+    const Groups G = slice_groups(items, n);
     for (int i = 0; i < n; ++i) {
+        if (G.group_of[(size_t)i] >= 0) continue;
         has_fp |= items[i].op == CT_OP_FP;
         has_bp |= items[i].op == CT_OP_BP || items[i].op == CT_OP_FBP;
     }

@@ -165,3 +165,76 @@ def test_config_validation(cuda):
         with pytest.raises(RuntimeError):
             ub.set_config(cfg)
     assert ub.config[1] is False
+
+
+def _make_groups(cuda, dtype):
+    """Three shared plans with three items of every operator each (slice
+    groups of three), plus two items whose plans appear once (the persistent
+    launches)."""
+    plans = [FanPlan(*G.uneven(k, scale=4), device=cuda) for k in range(3)]
+    singles = [FanPlan(*G.uneven(k, scale=4), device=cuda) for k in (3, 4)]
+    items, ref = [], []
+    ops = ("fp", "bp", "fbp", "fbp_adjoint")
+    seed = 0
+    for plan in plans:
+        for op in ops:
+            for _ in range(3):
+                seed += 1
+                items.append(_item(cuda, plan, op, dtype, seed, ref))
+    items.append(_item(cuda, singles[0], "fp", dtype, 99, ref))
+    items.append(_item(cuda, singles[1], "fbp", dtype, 98, ref))
+    return items, ref
+
+
+def _item(cuda, plan, op, dtype, seed, ref):
+    g = plan.geom
+    img = torch.from_numpy(phantom.ellipse_phantom(g.nx, float(g.dx), seed=seed)).to(cuda)
+    x = img if op in ("fp", "fbp_adjoint") else plan.fp(img)[0]
+    x = x.to(dtype).contiguous()
+    out_shape = plan.sino_shape if op in ("fp", "fbp_adjoint") else plan.image_shape
+    y = torch.full(out_shape, float("nan"), device=cuda, dtype=dtype)
+    ref.append({"fp": plan.fp, "bp": plan.bp, "fbp": plan.fbp,
+                "fbp_adjoint": plan.fbp_adjoint}[op](x.float())[0])
+    return plan, op, x, y
+
+
+def test_batch_slice_groups_equal_per_plan_operators(cuda):
+    items, ref = _make_groups(cuda, torch.float32)
+    ub = UnevenBatch(items)
+    ub.run()
+    for (plan, op, x, y), want in zip(items, ref):
+        if op == "fbp_adjoint":
+            assert rel_l2(_np(y), _np(want)) <= _tol(op), op
+        else:  # the same kernels on the same slices: identical bits
+            np.testing.assert_array_equal(_np(y), _np(want), err_msg=op)
+    # replayed from a graph, and after tuning (only the two persistent items
+    # have launch shapes), the results stay the same
+    ub.tune(reps=1)
+    ub.capture()
+    for _, _, _, y in items:
+        y.fill_(float("nan"))
+    ub.replay()
+    for (plan, op, x, y), want in zip(items, ref):
+        assert rel_l2(_np(y), _np(want)) <= _tol(op), op
+
+
+def test_batch_slice_groups_bf16(cuda):
+    items, ref = _make_groups(cuda, torch.bfloat16)
+    UnevenBatch(items).run()
+    for (plan, op, x, y), want in zip(items, ref):
+        # FP32 arithmetic on the BF16 input, the result rounded to BF16 once
+        if op != "fbp_adjoint":
+            np.testing.assert_array_equal(_np(y), _np(want.to(torch.bfloat16)), err_msg=op)
+        assert rel_l2(_np(y), _np(want)) <= 8e-3, op
+
+
+def test_batch_all_grouped_tunes(cuda):
+    plan = FanPlan(*G.uneven(1, scale=4), device=cuda)
+    ref = []
+    items = [_item(cuda, plan, "fp", torch.float32, s, ref) for s in range(4)]
+    ub = UnevenBatch(items)
+    cfg = ub.tune(reps=1)  # nothing persistent to time: the defaults come back
+    assert cfg["fp_blocks_per_sm"] > 0
+    ub.run()
+    for (_, _, _, y), want in zip(items, ref):
+        np.testing.assert_array_equal(_np(y), _np(want))
