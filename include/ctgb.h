@@ -343,7 +343,11 @@ ct_status ct_batch_workspace_size(const ct_batch_item *items, int n, size_t *byt
  * operators: one launch builds every FP item's quad images, one persistent
  * launch projects all FP items, the FBP / FBP-adjoint items are filtered with
  * their plans' filters, and one persistent launch backprojects all BP / FBP
- * items.  Item descriptors are passed as kernel parameters, so the call makes
+ * items.  Two or more items with the same plan (the same ct_plan handle),
+ * operator and dtype form a slice group: they are gathered into the
+ * workspace and run through the plan's multi-slice kernels (as ct_fp_fan,
+ * ct_bp_fan, ct_fbp_fan, ct_fbp_fan_adjoint on the group), so give slices of
+ * one geometry one plan.  Item descriptors are passed as kernel parameters, so the call makes
  * no host-to-device copy and can be captured in a CUDA graph (pass d_work; the
  * first call of a process should come before capture).  All plans must be on
  * one device.  d_work == NULL allocates stream-ordered, as the operators do.
