@@ -293,6 +293,34 @@ def test_utils_shim_numpy_and_torch(cuda):
     assert xt.grad is not None and torch.isfinite(xt.grad).all()
 
 
+def test_utils_large_host_batches(cuda):
+    """The reference-named entry points on a 40-slice host batch (numpy and
+    CPU tensors) equal the device-resident operators bit for bit; a shape
+    attribute that does not hold the result is refused."""
+    from fanbeamctrecon_tensorflowop_gb300 import utils
+    p, a = G.small()
+    plan = FanPlan(p, a, device=cuda)
+    g = plan.geom
+    nb = 40
+    img = _images(g, nb, seed=3)
+    sino = _sinos(g, nb, seed=4)
+    vs, ps = [nb, g.nx, g.ny], [nb, g.n_views, g.n_cols]
+    kw = dict(angle=a, parameter=p, vol_shape=vs, proj_shape=ps)
+    got = utils.fp_fan_curve(volume=img, **kw)
+    assert isinstance(got, np.ndarray) and got.shape == tuple(ps)
+    np.testing.assert_array_equal(got, plan.fp(_t(img, cuda)).cpu().numpy())
+    got = utils.bp_fan_curve(projection=torch.from_numpy(sino), **kw)
+    assert isinstance(got, torch.Tensor) and not got.is_cuda and got.shape == tuple(vs)
+    np.testing.assert_array_equal(got.numpy(), plan.bp(_t(sino, cuda)).cpu().numpy())
+    got = utils.fbp_fan_curve(projection=sino, **kw)
+    np.testing.assert_array_equal(got, plan.fbp(_t(sino, cuda)).cpu().numpy())
+    got = utils.back_projection(projection=sino, **kw)
+    np.testing.assert_array_equal(got, plan.fdk_bp(_t(sino, cuda)).cpu().numpy())
+    with pytest.raises(ValueError):
+        utils.fp_fan_curve(volume=img, angle=a, parameter=p, vol_shape=vs,
+                           proj_shape=[nb - 1, g.n_views, g.n_cols])
+
+
 def test_config1_against_oracle(cuda, orc):
     """The clinical-scale geometry (512^2, 984 x 888): FP of the seeded
     phantom, Shepp-Logan FBP of that sinogram, BP of a U[0,1) sinogram."""
