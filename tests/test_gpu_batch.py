@@ -238,3 +238,25 @@ def test_batch_all_grouped_tunes(cuda):
     ub.run()
     for (_, _, _, y), want in zip(items, ref):
         np.testing.assert_array_equal(_np(y), _np(want))
+
+
+def test_batch_slice_groups_with_preweights(cuda):
+    """Slice groups of short-scan (Parker) and cosine-weighted plans: the
+    grouped FBP and FBP adjoint apply the pre-weights as ct_fbp_fan and
+    ct_fbp_fan_adjoint do."""
+    p, a = G.short_scan(n=96, views=160, cols=256)
+    plans = [FanPlan(p, a, device=cuda, short_scan=True),
+             FanPlan(p, a, device=cuda, cosine_weight=True)]
+    items, ref = [], []
+    seed = 100
+    for plan in plans:
+        for op in ("fbp", "fbp_adjoint"):
+            for _ in range(3):
+                seed += 1
+                items.append(_item(cuda, plan, op, torch.float32, seed, ref))
+    UnevenBatch(items).run()
+    for (plan, op, x, y), want in zip(items, ref):
+        if op == "fbp":
+            np.testing.assert_array_equal(_np(y), _np(want), err_msg=op)
+        else:
+            assert rel_l2(_np(y), _np(want)) <= _tol(op), op
