@@ -6,7 +6,7 @@
 // taps of every cell), then fp_warp (fp_body.cuh) walks 32 adjacent rays of a
 // view per warp, row-synchronously, summing each cell's samples in closed
 // form (cellwalk.cuh): one 16-byte gather per cell instead of four per
-// sample.  Eight slices share one walk.  Output:
+// sample.  Up to 16 slices share one walk.  Output:
 // p = 0.125*dx * sum_k bilinear_clamp(img, start + k*step), k < n.
 #include <cfloat>
 #include <climits>
