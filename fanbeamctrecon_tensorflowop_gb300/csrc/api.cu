@@ -1,5 +1,7 @@
 // The C ABI (include/ctgb.h): argument validation, plans, workspace, dispatch.
+#include <algorithm>
 #include <atomic>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -56,6 +58,10 @@ ct_status acquire(Workspace &w, void *given, size_t given_bytes, size_t need, cu
             g_last_error = "workspace smaller than ct_workspace_size";
             return CT_ERR_WORKSPACE;
         }
+        if (reinterpret_cast<uintptr_t>(given) % 16) {
+            g_last_error = "workspace not 16-byte aligned";
+            return CT_ERR_WORKSPACE;
+        }
         w.ptr = given;
         return CT_OK;
     }
@@ -81,6 +87,13 @@ size_t proj_bytes(const ct_plan *p, int batch) {
     return sizeof(float) * (size_t)batch * p->g.n_views * p->n_rows * p->g.n_cols;
 }
 
+// where the FDK adjoint's transpose work starts (after its projection
+// copies, 256-byte aligned)
+size_t fdk_adjoint_work_offset(const ct_plan *p, int batch) {
+    const size_t copies = ctk::has_preweight(p) ? 2 : 1;
+    return (copies * proj_bytes(p, batch) + 255) & ~(size_t)255;
+}
+
 size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
     const size_t parker = ctk::has_preweight(p) ? 2 : 1;  // weighted copy + filtered copy
     switch (op) {
@@ -88,8 +101,8 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
             return ctk::cone_fp_work_bytes(p, batch);
         case CT_OP_FDK_CONE:
             return parker * proj_bytes(p, batch);
-        case CT_OP_FDK_CONE_ADJOINT:  // + the transpose's per-volume maxima
-            return parker * proj_bytes(p, batch) + ctk::cone_bp_transpose_work_bytes(batch);
+        case CT_OP_FDK_CONE_ADJOINT:  // + the transpose's own work
+            return fdk_adjoint_work_offset(p, batch) + ctk::cone_bp_transpose_work_bytes(p, batch);
         case CT_OP_FP:
             return ctk::fp_fan_work_bytes(p, batch);
         case CT_OP_FP_ADJOINT:
@@ -265,6 +278,11 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
         }
     p->n_rows = n_rows;
     p->nz = nz;
+    p->view_z_min = p->view_z_max = 0.0f;
+    for (size_t v = 0; v < t.view_z.size(); ++v) {
+        p->view_z_min = v ? std::min(p->view_z_min, t.view_z[v]) : t.view_z[v];
+        p->view_z_max = v ? std::max(p->view_z_max, t.view_z[v]) : t.view_z[v];
+    }
     p->total_samples = t.total_samples;
     p->max_nsamp = t.max_nsamp;
     p->h_view_cs = t.view_cs;
@@ -535,9 +553,8 @@ ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_
                  stream);
     if (st != CT_OK) return st;
     float *tmp = static_cast<float *>(w.ptr);
-    void *maxima = static_cast<char *>(w.ptr) + (ctk::has_preweight(plan) ? 2 : 1) *
-                                                    proj_bytes(plan, batch);
-    st = launch_status(ctk::cone_bp_transpose(plan, d_vol, tmp, batch, maxima, stream),
+    void *twork = static_cast<char *>(w.ptr) + fdk_adjoint_work_offset(plan, batch);
+    st = launch_status(ctk::cone_bp_transpose(plan, d_vol, tmp, batch, twork, stream),
                        "ct_fdk_cone_adjoint");
     if (st != CT_OK) return st;
     const int rows = batch * plan->g.n_views * plan->n_rows;

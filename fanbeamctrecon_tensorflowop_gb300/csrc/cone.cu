@@ -33,8 +33,10 @@ struct ConeArgs {
     double fov_r2;
     float coef[9];
     int atan_deg;
-    // fixed-point bounds of the transpose (see cone_bp_transpose_kernel)
-    float fix_npix, fix_slices, fix_wmax;
+    // fixed-point bounds of the transposes (see cone_bp_transpose_kernel);
+    // fix_edge: slices that can reach the first or last row (nz when samples
+    // can clamp onto them, fix_slices otherwise)
+    float fix_npix, fix_slices, fix_wmax, fix_edge;
 };
 
 template <int DEG>
@@ -67,6 +69,15 @@ __device__ __forceinline__ float4 tex_weights2d(float A, float B) {
     return make_float4(256.0f - A - B + w11, A - w11, B - w11, w11);
 }
 
+// Slices per thread of cone_bp_kernel.  The row coordinate of slice k is
+// formed from the height of its group's first slice, group_z(k & ~(kZC-1)),
+// plus (k mod kZC) row steps; the transpose forms it the same way, so both
+// sample each slice at the same fp32 row coordinate.
+constexpr int kZC = 16;
+__device__ __forceinline__ float group_z(const ConeArgs &a, int k0) {
+    return fmaf(a.dz, (float)k0 + 0.5f, a.zmin);
+}
+
 // ---- CB_EA backprojection ----------------------------------------------------
 // Thread = one (x, y) pixel and ZC consecutive z slices; block = 32 x 8 pixels.
 // Per view the column, the 1/(U^2+t^2) weight and the row slope are computed
@@ -92,7 +103,7 @@ __global__ void __launch_bounds__(kThreads)
     const size_t pview = (size_t)a.n_rows * a.C;
     if (__syncthreads_or(in) && in) {
         const float *pb = proj + (size_t)b * a.V * pview;
-        const float z0 = a.zmin + a.dz * ((float)k0 + 0.5f);
+        const float z0 = group_z(a, k0);
         const float rmax = (float)a.n_rows;
         for (int v = 0; v < a.V; ++v) {
             const float2 cs = __ldg(view_cs + v);
@@ -300,6 +311,249 @@ __global__ void __launch_bounds__(256)
         m = fmaxf(m, fabsf(__ldg(vb + e)));
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(vmax_bits + blockIdx.y, __float_as_int(m));
+}
+
+// ---- CB_EA transpose, lanes along z --------------------------------------------
+// Used when all detector rows of a view fit in shared memory.  Block = one
+// view of one volume, with its [C][n_rows] fixed-point accumulators
+// (column-major with an odd column stride, so that neither the lanes' row
+// updates nor the write-out across a row conflict in the banks).  A lane
+// takes 8 consecutive slices of one pixel, read as two float4 from a z-major
+// copy of the volume; a warp takes 32 / 2^lg pixels of an image row (2^lg
+// lanes per pixel, 4 pixels for 64 slices).  Along its slices a lane's
+// detector rows only move forward, so it keeps the last row it touched in
+// registers and adds each row to shared memory once it is complete: for a
+// row step of about one row per slice that is two atomics per slice instead
+// of four.  Row indices and weights follow cone_bp_kernel exactly (rows
+// clamped onto the first and last row included).  Rows 0 and n_rows-1 are
+// kept at a fixed-point scale whose bound counts all nz slices where samples
+// can clamp onto them, the other rows at the fine one.
+#ifndef CT_CONE_ZT_THREADS
+#define CT_CONE_ZT_THREADS 1024
+#endif
+constexpr int kZThreads = CT_CONE_ZT_THREADS;
+constexpr int kZS = 8;  // consecutive slices per lane
+
+// [B][nz][ny*nx] -> [B][ny*nx][nzp] (nzp = nz rounded up to kZS, zero-filled),
+// and per volume max |vol| into vmax_bits (which must start at zero).
+__global__ void __launch_bounds__(256)
+    cone_zmajor_kernel(const float *__restrict__ vol, float *__restrict__ vol_t,
+                       int *vmax_bits, int nz, int npix, int nzp) {
+    __shared__ float tile[32][33];
+    const int p0 = blockIdx.x * 32, kc = blockIdx.y * 32, b = blockIdx.z;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const float *vb = vol + (size_t)b * nz * npix;
+    float m = 0.0f;
+#pragma unroll
+    for (int j = ty; j < 32; j += 8) {
+        const int k = kc + j, p = p0 + tx;
+        const float x = (k < nz && p < npix) ? __ldg(vb + (size_t)k * npix + p) : 0.0f;
+        tile[j][tx] = x;
+        m = fmaxf(m, fabsf(x));
+    }
+    __syncthreads();
+    float *tb = vol_t + (size_t)b * npix * nzp;
+#pragma unroll
+    for (int j = ty; j < 32; j += 8) {
+        const int p = p0 + j;
+        if (p < npix && kc + tx < nzp) tb[(size_t)p * nzp + kc + tx] = tile[tx][j];
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (tx == 0 && m > 0.0f) atomicMax(vmax_bits + b, __float_as_int(m));
+}
+
+// Per image row iy: the fp32 pixel centre py[iy] and the span [lo, hi) of
+// columns whose centres lie in the FOV disc (an interval: the test is
+// monotone in |x|); px[ix] likewise.  Same double expressions as
+// cone_bp_kernel's FOV test, so both select the same pixels.
+__global__ void __launch_bounds__(32)
+    cone_fov_tables_kernel(ConeArgs a, float *__restrict__ px_tab, float *__restrict__ py_tab,
+                           int2 *__restrict__ span) {
+    const int iy = blockIdx.x, lane = threadIdx.x;
+    const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
+    int lo = INT_MAX, hi = -1;
+    for (int x0 = 0; x0 < a.nx; x0 += 32) {
+        const int ix = x0 + lane;
+        const double xd = (double)a.xmin + (double)a.dx * (ix + 0.5);
+        if (ix < a.nx && (xd * xd + yd * yd <= a.fov_r2)) {
+            lo = min(lo, ix);
+            hi = max(hi, ix);
+        }
+        if (iy == 0 && ix < a.nx) px_tab[ix] = (float)xd;
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lane == 0) {
+        span[iy] = hi >= 0 ? make_int2(lo, hi + 1) : make_int2(0, 0);
+        py_tab[iy] = (float)yd;
+    }
+}
+
+// A warp's pixels: image rows in order, in each the tiles of `per` pixels
+// t = (warp + iy) mod NW + NW m of the row's FOV span [x0, end).
+struct ZtCursor {
+    int iy, t, ntile, x0, end;
+    __device__ __forceinline__ bool next(const int2 *__restrict__ span, int ny, int warp, int nw,
+                                         int per) {
+        t += nw;
+        while (t >= ntile) {
+            if (++iy >= ny) return false;
+            const int2 sp = __ldg(span + iy);
+            x0 = sp.x;
+            end = sp.y;
+            ntile = (sp.y - sp.x + per - 1) / per;
+            t = (warp + iy) % nw;
+        }
+        return true;
+    }
+};
+
+template <int DEG, bool TEX>
+__global__ void __launch_bounds__(kZThreads, 1)
+    cone_bp_transpose_z_kernel(const float *__restrict__ vol_t, float *__restrict__ proj,
+                               const float2 *__restrict__ view_cs,
+                               const float *__restrict__ view_z, const int *__restrict__ vmax_bits,
+                               const float *__restrict__ px_tab, const float *__restrict__ py_tab,
+                               const int2 *__restrict__ span, ConeArgs a, int nzp, int lg) {
+    extern __shared__ int4 acc4[];
+    int *acc = reinterpret_cast<int *>(acc4);
+    const int ld = a.n_rows | 1;
+    const int nacc4 = (a.C * ld + 3) / 4;
+    for (int k = threadIdx.x; k < nacc4; k += kZThreads) acc4[k] = make_int4(0, 0, 0, 0);
+    const int v = blockIdx.x, b = blockIdx.y;
+    const float vmax = __int_as_float(__ldg(vmax_bits + b));
+    const float bound = a.fix_npix * a.fix_slices * a.fix_wmax * vmax;
+    const float scale = bound > 0.0f ? 1073741824.0f / bound : 0.0f;
+    const float bound_c = a.fix_npix * a.fix_edge * a.fix_wmax * vmax;
+    const float scale_c = bound_c > 0.0f ? 1073741824.0f / bound_c : 0.0f;
+    __syncthreads();
+    const float2 cs = __ldg(view_cs + v);
+    const float zs = view_z ? __ldg(view_z + v) : 0.0f;
+    const float rmax = (float)a.n_rows;
+    const int last = a.n_rows - 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NW = kZThreads / 32;
+    const int gp = 1 << lg, per = 32 >> lg;  // lanes per pixel, pixels per warp
+    const int slot = lane >> lg, g = lane & (gp - 1);
+    const int G = nzp / kZS;                 // slice groups per pixel
+    const float *vb = vol_t + (size_t)b * a.nx * a.ny * nzp;
+    const float4 zero4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    auto load = [&](const ZtCursor &c, float4 &x0, float4 &x1) {
+        const int ix = c.x0 + c.t * per + slot;
+        x0 = x1 = zero4;
+        if (ix < c.end && g < G) {
+            const float4 *q = reinterpret_cast<const float4 *>(
+                vb + ((size_t)c.iy * a.nx + ix) * nzp + g * kZS);
+            x0 = __ldg(q);
+            x1 = __ldg(q + 1);
+        }
+    };
+    ZtCursor cur{-1, 0, 0, 0, 0};
+    bool have = cur.next(span, a.ny, warp, NW, per);
+    float4 va = zero4, vc = zero4;  // this lane's 8 slices of the current pixel
+    if (have) load(cur, va, vc);
+    while (have) {
+        // the next tile's loads go out before this tile's work
+        ZtCursor nxt = cur;
+        const bool more = nxt.next(span, a.ny, warp, NW, per);
+        float4 na = zero4, nc = zero4;
+        if (more) load(nxt, na, nc);
+        const int ix = cur.x0 + cur.t * per + slot;
+        if (ix < cur.end && g < G) {
+            const float px = __ldg(px_tab + ix), py = __ldg(py_tab + cur.iy);
+            const float U = fmaf(px, cs.x, fmaf(py, cs.y, a.R));
+            const float t = fmaf(py, cs.x, -px * cs.y);
+            const float rU = __fdividef(1.0f, U);
+            const float y = fmaf(cone_atan<DEG>(t * rU, a), a.inv_dcol, a.pos_off);
+            if (y > 0.5f && y < a.fC + 0.5f) {
+                int ic;
+                float f;
+                split_pos(y, ic, f);
+                const float A = floorf(fmaf(f, 256.0f, 0.5f));  // used with TEX only
+                int *c0 = acc + max(ic - 1, 0) * ld;
+                int *c1 = acc + min(ic, a.C - 1) * ld;
+                const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
+                const float slope = a.row_scale * rU;
+                const float drr = a.dz * slope;
+                auto emit = [&](int row, float x0, float x1) {
+                    const float sc = (unsigned)(row - 1) < (unsigned)(last - 1) ? scale : scale_c;
+                    atomicAdd(c0 + row, __float2int_rn(x0 * sc));
+                    atomicAdd(c1 + row, __float2int_rn(x1 * sc));
+                };
+                // passes of gp groups (one pass unless nz > 32 * kZS)
+                for (int kb = g * kZS; kb < a.nz; kb += gp * kZS) {
+                    float x[kZS];
+                    if (kb == g * kZS) {
+                        x[0] = va.x, x[1] = va.y, x[2] = va.z, x[3] = va.w;
+                        x[4] = vc.x, x[5] = vc.y, x[6] = vc.z, x[7] = vc.w;
+                    } else {
+                        const float4 *q = reinterpret_cast<const float4 *>(
+                            vb + ((size_t)cur.iy * a.nx + ix) * nzp + kb);
+                        const float4 u0 = __ldg(q), u1 = __ldg(q + 1);
+                        x[0] = u0.x, x[1] = u0.y, x[2] = u0.z, x[3] = u0.w;
+                        x[4] = u1.x, x[5] = u1.y, x[6] = u1.z, x[7] = u1.w;
+                    }
+                    // the lane's slices lie in one group of kZC (kZS divides kZC)
+                    const int kg = kb & ~(kZC - 1);
+                    const float rr0 = fmaf(group_z(a, kg) - zs, slope, a.row_off);
+                    const float kk0 = (float)(kb - kg);
+                    int prow = -1;  // the pending row and its two column sums
+                    float p0 = 0.0f, p1 = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < kZS; ++j) {
+                        // (slices beyond nz read zero and add nothing)
+                        const float rr =
+                            fminf(fmaxf(fmaf(kk0 + (float)j, drr, rr0), 0.0f), rmax + 0.5f);
+                        int ir;
+                        float fr;
+                        split_pos(rr, ir, fr);
+                        const int lo = min(max(ir - 1, 0), last), hi = min(ir, last);
+                        const float vw = x[j] * wgt;
+                        float l0, l1, h0, h1;  // (lo, i0), (lo, i1), (hi, i0), (hi, i1)
+                        if constexpr (TEX) {
+                            const float4 w = tex_weights2d(A, floorf(fmaf(fr, 256.0f, 0.5f)));
+                            const float s = vw * (1.0f / 256.0f);
+                            l0 = s * w.x;
+                            l1 = s * w.y;
+                            h0 = s * w.z;
+                            h1 = s * w.w;
+                        } else {
+                            const float hb = vw * fr, lb = vw - hb;
+                            l0 = lb * (1.0f - f);
+                            l1 = lb * f;
+                            h0 = hb * (1.0f - f);
+                            h1 = hb * f;
+                        }
+                        const bool flush = prow != lo;
+                        if (flush && prow >= 0) emit(prow, p0, p1);
+                        const float q0 = flush ? l0 : p0 + l0, q1 = flush ? l1 : p1 + l1;
+                        if (hi == lo) {  // both row taps on one row (clamped): keep it
+                            p0 = q0 + h0;
+                            p1 = q1 + h1;
+                        } else {
+                            emit(lo, q0, q1);
+                            p0 = h0;
+                            p1 = h1;
+                        }
+                        prow = hi;
+                    }
+                    emit(prow, p0, p1);
+                }
+            }
+        }
+        va = na;
+        vc = nc;
+        cur = nxt;
+        have = more;
+    }
+    __syncthreads();
+    float *pv = proj + ((size_t)b * a.V + v) * a.n_rows * a.C;
+    const float inv = scale > 0.0f ? bound * (1.0f / 1073741824.0f) : 0.0f;
+    const float inv_c = scale_c > 0.0f ? bound_c * (1.0f / 1073741824.0f) : 0.0f;
+    for (int e = threadIdx.x; e < a.n_rows * a.C; e += kZThreads) {
+        const int r = e / a.C, c = e - r * a.C;
+        pv[e] = (float)acc[c * ld + r] * ((unsigned)(r - 1) < (unsigned)(last - 1) ? inv : inv_c);
+    }
 }
 
 // ---- cone-beam forward projection -----------------------------------------------
@@ -593,7 +847,7 @@ ConeArgs make_cone_args(const ct_plan *p) {
 
 int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream) {
     const ConeArgs a = make_cone_args(p);
-    constexpr int ZC = 16;
+    constexpr int ZC = kZC;
     const int zgroups = (a.nz + ZC - 1) / ZC;
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
     for (int b0 = 0; b0 < batch; b0 += 4096) {
@@ -612,10 +866,60 @@ int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *st
     return (int)cudaGetLastError();
 }
 
-size_t cone_bp_transpose_work_bytes(int batch) { return sizeof(int) * (size_t)batch; }
+namespace {
+
+size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// shared-memory accumulators of the lanes-along-z transpose (0: does not fit)
+size_t zt_smem(const ct_plan *p) {
+    const size_t ints = ((size_t)p->g.n_cols * (size_t)(p->n_rows | 1) + 3) & ~(size_t)3;
+    return sizeof(int) * ints <= 227 * 1024 ? sizeof(int) * ints : 0;
+}
+
+int zt_nzp(const ct_plan *p) { return (p->nz + kZS - 1) / kZS * kZS; }
+
+// log2 of the lanes per pixel: slice groups rounded up to a power of two, <= 32
+int zt_lg(const ct_plan *p) {
+    const int groups = zt_nzp(p) / kZS;
+    int lg = 0;
+    while ((1 << lg) < groups && lg < 5) ++lg;
+    return lg;
+}
+
+// Work of the transpose: per-volume maxima, then (lanes-along-z path) the
+// pixel tables and the z-major copy of the volumes.
+struct ZtWork {
+    size_t vmax, px, py, span, vol_t, total;
+};
+
+ZtWork zt_work(const ct_plan *p, int batch) {
+    ZtWork w{};
+    w.vmax = 0;
+    size_t o = align256(sizeof(int) * (size_t)batch);
+    if (!zt_smem(p)) {
+        w.total = o;
+        return w;
+    }
+    w.px = o;
+    o += align256(sizeof(float) * (size_t)p->g.nx);
+    w.py = o;
+    o += align256(sizeof(float) * (size_t)p->g.ny);
+    w.span = o;
+    o += align256(sizeof(int2) * (size_t)p->g.ny);
+    w.vol_t = o;
+    o += sizeof(float) * (size_t)batch * p->g.nx * p->g.ny * zt_nzp(p);
+    w.total = o;
+    return w;
+}
+
+}  // namespace
+
+size_t cone_bp_transpose_work_bytes(const ct_plan *p, int batch) {
+    return zt_work(p, batch).total;
+}
 
 bool cone_bp_transpose_supported(const ct_plan *p) {
-    return sizeof(int) * (kRB + 2) * (size_t)p->g.n_cols <= 227 * 1024;
+    return zt_smem(p) || sizeof(int) * (kRB + 2) * (size_t)p->g.n_cols <= 227 * 1024;
 }
 
 int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *work,
@@ -632,17 +936,57 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
         // slice centres within one row (drow L / D at the detector) either side
         a.fix_slices = (float)(2.0 * (double)p->g.drow * (R + rf) / (D * (double)p->g.dz) + 2.0);
         a.fix_wmax = (float)(1.0 / ((R - rf) * (R - rf)));
+        // row + 1/2 = z row_scale / U + row_off over the slice centres
+        // relative to every source height and U in [R - rf, R + rf]; no
+        // clamping when it stays inside [1, n_rows) with a margin
+        const double z0 = (double)a.zmin + 0.5 * p->g.dz - p->view_z_max;
+        const double z1 = -(double)a.zmin - 0.5 * p->g.dz - p->view_z_min;
+        const double rs = (double)p->g.sdd / p->g.drow, ro = a.row_off;
+        const double lo = ro + rs * (z0 < 0.0 ? z0 / (R - rf) : z0 / (R + rf));
+        const double hi = ro + rs * (z1 > 0.0 ? z1 / (R - rf) : z1 / (R + rf));
+        const bool clamps = !(lo >= 1.01 && hi <= p->n_rows - 0.01);
+        a.fix_edge = clamps ? (float)a.nz : a.fix_slices;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    int *vmax_bits = static_cast<int *>(work);
+    const ZtWork zw = zt_work(p, batch);
+    char *wb = static_cast<char *>(work);
+    int *vmax_bits = reinterpret_cast<int *>(wb + zw.vmax);
     cudaError_t e0 = cudaMemsetAsync(vmax_bits, 0, sizeof(int) * (size_t)batch, s);
     if (e0 != cudaSuccess) return (int)e0;
+    const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
+    const bool tex = p->opts.texture_weights != 0;
     const size_t per_volume = (size_t)a.nz * a.ny * a.nx;
+    if (const size_t smem = zt_smem(p)) {
+        const int npix = a.nx * a.ny, nzp = zt_nzp(p);
+        float *px = reinterpret_cast<float *>(wb + zw.px);
+        float *py = reinterpret_cast<float *>(wb + zw.py);
+        int2 *span = reinterpret_cast<int2 *>(wb + zw.span);
+        float *vol_t = reinterpret_cast<float *>(wb + zw.vol_t);
+        cone_fov_tables_kernel<<<a.ny, 32, 0, s>>>(a, px, py, span);
+        ct_count_launch();
+        auto kern = a.atan_deg == 4   ? (tex ? cone_bp_transpose_z_kernel<4, true>
+                                             : cone_bp_transpose_z_kernel<4, false>)
+                    : a.atan_deg == 8 ? (tex ? cone_bp_transpose_z_kernel<8, true>
+                                             : cone_bp_transpose_z_kernel<8, false>)
+                                      : (tex ? cone_bp_transpose_z_kernel<0, true>
+                                             : cone_bp_transpose_z_kernel<0, false>);
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+        for (int b0 = 0; b0 < batch; b0 += 65535) {
+            const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+            cone_zmajor_kernel<<<dim3((npix + 31) / 32, (nzp + 31) / 32, nb), 256, 0, s>>>(
+                vol + (size_t)b0 * per_volume, vol_t, vmax_bits + b0, a.nz, npix, nzp);
+            kern<<<dim3(a.V, nb), kZThreads, smem, s>>>(
+                vol_t, proj + (size_t)b0 * a.V * a.n_rows * a.C, vcs, p->d_view_z,
+                vmax_bits + b0, px, py, span, a, nzp, zt_lg(p));
+            ct_count_launch(2);
+        }
+        return (int)cudaGetLastError();
+    }
     volume_absmax_kernel<<<dim3(152, batch), 256, 0, s>>>(vol, per_volume, vmax_bits);
     ct_count_launch();
-    const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
     const size_t smem = sizeof(int) * (kRB + 2) * a.C;
-    const bool tex = p->opts.texture_weights != 0;
     auto kern = a.atan_deg == 4
                     ? (tex ? cone_bp_transpose_kernel<4, true> : cone_bp_transpose_kernel<4, false>)
                 : a.atan_deg == 8

@@ -59,6 +59,7 @@ struct ct_plan {
     float fp_weight;                 // 0.125*dx (FP/transform.cu:144)
     float fov_r2;                    // rfov^2 (BP/transform.cu:116)
     int n_rows, nz;                  // cone plans; 1 and 1 for fan plans
+    float view_z_min, view_z_max;    // range of the source heights (0, 0 without them)
     int atan_deg;                    // 4 or 8: polynomial atan on the FOV; 0: atanf
     float atan_coef[9];
     int gather_atan_deg;             // the same fit on the FOV widened by 1.5 pixels
@@ -110,8 +111,10 @@ inline bool has_preweight(const ct_plan *p) { return p->d_parker || p->d_cosw; }
 // [batch][V][n_rows][C]
 int apply_preweight(const ct_plan *p, const float *in, float *out, int batch, void *stream);
 int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream);
-// work: cone_bp_transpose_work_bytes(batch) bytes (per-volume max |vol|)
-size_t cone_bp_transpose_work_bytes(int batch);
+// work: cone_bp_transpose_work_bytes(p, batch) bytes (per-volume max |vol|;
+// where every detector row of a view fits in shared memory, also pixel tables
+// and a z-major copy of the volumes)
+size_t cone_bp_transpose_work_bytes(const ct_plan *p, int batch);
 bool cone_bp_transpose_supported(const ct_plan *p);  // its detector rows fit in shared memory
 int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch, void *work,
                       void *stream);

@@ -200,7 +200,8 @@ ct_status ct_plan_geom(const ct_plan *plan, ct_fan_geom *out);
 
 /* Device scratch bytes an operator needs for `batch` slices.  Operators that
  * take d_work accept d_work == NULL, in which case they allocate the scratch
- * stream-ordered (cudaMallocAsync/cudaFreeAsync) on `stream`. */
+ * stream-ordered (cudaMallocAsync/cudaFreeAsync) on `stream`.  A given d_work
+ * must be 16-byte aligned (CT_ERR_WORKSPACE otherwise). */
 ct_status ct_workspace_size(const ct_plan *plan, ct_op op, int batch, size_t *bytes);
 
 /* ---- fan-beam operators ---------------------------------------------------- */

@@ -86,6 +86,44 @@ def test_fdk_adjoint(cone, cuda, orc):
     assert m <= DOT_TOL, m
 
 
+TRANSPOSE_CASES = {
+    # 45 slices (two 32-slice chunks of the lanes-along-z kernel) on a detector
+    # a third as tall as the magnified volume: samples clamp onto both edge rows
+    "tall_clamped": lambda: G.cone_small(n=30, views=40, cols=60, n_rows=20, nz=45, pixel=6.0,
+                                         dz=2.0, drow=3.0),
+    # more detector rows than one view's accumulators fit in shared memory:
+    # the row-block kernel
+    "rows_beyond_shared_memory": lambda: G.cone_small(n=24, views=20, cols=64, n_rows=1000, nz=6,
+                                                      drow=0.1),
+}
+
+
+@pytest.mark.parametrize("tex", [False, True])
+@pytest.mark.parametrize("case", list(TRANSPOSE_CASES))
+def test_fdk_adjoint_kernel_paths(cuda, orc, case, tex):
+    """Both CB_EA transpose kernels against the oracle (texture weights: the
+    filtered adjoint's 2e-3, as the fan-beam FBP adjoint) and the dot test."""
+    p, a, nr, nz = TRANSPOSE_CASES[case]()
+    plan = ConePlan(p, a, nr, nz, device=cuda, texture_weights=tex)
+    g = orc.decode(p)
+    x = _vol(g, nz, 2, seed=9)
+    orc.set_texture_emulation(tex)
+    try:
+        ref = orc.fdk_cone_adjoint(g, nr, nz, a, x)
+    finally:
+        orc.set_texture_emulation(False)
+    got = _np(plan.fdk_adjoint(_t(x, cuda)))
+    assert rel_l2(got, ref) <= (2e-3 if tex else TOL), rel_l2(got, ref)
+    rng = np.random.default_rng(2)
+    xx = rng.standard_normal((2, nz, g.ny, g.nx)).astype(np.float32)
+    yy = rng.standard_normal((2, g.n_views, nr, g.n_cols)).astype(np.float32)
+    ax = _np(plan.fdk_adjoint(_t(xx, cuda)))
+    aty = _np(plan.fdk(_t(yy, cuda)))
+    m = abs(float(np.vdot(ax, yy)) - float(np.vdot(xx, aty))) / (
+        np.linalg.norm(ax) * np.linalg.norm(yy))
+    assert m <= DOT_TOL, m
+
+
 def test_fdk_cone_single_row_matches_fan_fdk_op(cuda):
     p, a = G.fdk_driver(nview=60, nimg=48)
     cone = ConePlan(p, a, 1, 1, device=cuda)
