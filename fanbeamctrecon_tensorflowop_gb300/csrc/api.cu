@@ -87,6 +87,13 @@ size_t proj_bytes(const ct_plan *p, int batch) {
     return sizeof(float) * (size_t)batch * p->g.n_views * p->n_rows * p->g.n_cols;
 }
 
+// where FDK's backprojection work starts (after its projection copies,
+// 256-byte aligned)
+size_t fdk_cone_work_offset(const ct_plan *p, int batch) {
+    const size_t copies = ctk::has_preweight(p) ? 2 : 1;
+    return (copies * proj_bytes(p, batch) + 255) & ~(size_t)255;
+}
+
 // where the FDK adjoint's transpose work starts (after its projection
 // copies, 256-byte aligned)
 size_t fdk_adjoint_work_offset(const ct_plan *p, int batch) {
@@ -99,8 +106,8 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
     switch (op) {
         case CT_OP_FP_CONE:
             return ctk::cone_fp_work_bytes(p, batch);
-        case CT_OP_FDK_CONE:
-            return parker * proj_bytes(p, batch);
+        case CT_OP_FDK_CONE:  // + the backprojection's quad images
+            return fdk_cone_work_offset(p, batch) + ctk::cone_bp_work_bytes(p);
         case CT_OP_FDK_CONE_ADJOINT:  // + the transpose's own work
             return fdk_adjoint_work_offset(p, batch) + ctk::cone_bp_transpose_work_bytes(p, batch);
         case CT_OP_FP:
@@ -508,7 +515,10 @@ ct_status ct_cone_bp(const ct_plan *plan, const float *d_proj, float *d_vol, int
     if (st != CT_OK || batch == 0) return st;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
-    return launch_status(ctk::cone_bp(plan, d_proj, d_vol, batch, stream), "ct_cone_bp");
+    Workspace w;
+    st = acquire(w, nullptr, 0, ctk::cone_bp_work_bytes(plan), stream);
+    if (st != CT_OK) return st;
+    return launch_status(ctk::cone_bp(plan, d_proj, d_vol, batch, w.ptr, stream), "ct_cone_bp");
 }
 
 ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,
@@ -535,7 +545,10 @@ ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, in
         ctk::ramp_filter(plan, src, filt, batch * plan->g.n_views * plan->n_rows, stream),
         "ct_fdk_cone");
     if (st != CT_OK) return st;
-    return launch_status(ctk::cone_bp(plan, filt, d_vol, batch, stream), "ct_fdk_cone");
+    void *bwork = ctk::cone_bp_work_bytes(plan)
+                      ? static_cast<char *>(w.ptr) + fdk_cone_work_offset(plan, batch)
+                      : nullptr;
+    return launch_status(ctk::cone_bp(plan, filt, d_vol, batch, bwork, stream), "ct_fdk_cone");
 }
 
 ct_status ct_fdk_cone_adjoint(const ct_plan *plan, const float *d_vol, float *d_proj, int batch,

@@ -73,7 +73,10 @@ __device__ __forceinline__ float4 tex_weights2d(float A, float B) {
 // formed from the height of its group's first slice, group_z(k & ~(kZC-1)),
 // plus (k mod kZC) row steps; the transpose forms it the same way, so both
 // sample each slice at the same fp32 row coordinate.
-constexpr int kZC = 16;
+#ifndef CT_CONE_ZC
+#define CT_CONE_ZC 16
+#endif
+constexpr int kZC = CT_CONE_ZC;
 __device__ __forceinline__ float group_z(const ConeArgs &a, int k0) {
     return fmaf(a.dz, (float)k0 + 0.5f, a.zmin);
 }
@@ -83,11 +86,21 @@ __device__ __forceinline__ float group_z(const ConeArgs &a, int k0) {
 // Per view the column, the 1/(U^2+t^2) weight and the row slope are computed
 // once; each slice then needs one row coordinate and a bilinear (col, row)
 // sample of the view (FDK/GPURecon_GPU.cu:33-47).
-template <int ZC, int DEG, bool TEX>
-__global__ void __launch_bounds__(kThreads)
-    cone_bp_kernel(const float *__restrict__ proj, float *__restrict__ vol,
-                   const float2 *__restrict__ view_cs, const float *__restrict__ view_z,
-                   ConeArgs a, int batch) {
+// QUAD: the samples come from the views' quad images (one volume), where cell
+// (ir, ic) holds the four clamped taps (r0, i0), (r0, i1), (r1, i0), (r1, i1)
+// of row and column positions ir, ic: one 16-byte load per sample instead of
+// four 4-byte gathers, the same four values.
+// 6 blocks of 256 threads per SM (40 registers): with QUAD, 17.9 ms per
+// clinical FDK volume, where the compiler's own choice (74-80 registers)
+// took 32.4 ms and 5 blocks 21.0 ms
+#ifndef CT_CONE_BP_MINB
+#define CT_CONE_BP_MINB 6
+#endif
+template <int ZC, int DEG, bool TEX, bool QUAD>
+__global__ void __launch_bounds__(kThreads, CT_CONE_BP_MINB)
+    cone_bp_kernel(const float *__restrict__ proj, const float4 *__restrict__ pq,
+                   float *__restrict__ vol, const float2 *__restrict__ view_cs,
+                   const float *__restrict__ view_z, ConeArgs a, int batch) {
     const int ix = blockIdx.x * 32 + threadIdx.x;
     const int iy = blockIdx.y * 8 + threadIdx.y;
     const int zgroups = (a.nz + ZC - 1) / ZC;
@@ -119,6 +132,7 @@ __global__ void __launch_bounds__(kThreads)
             const int i0 = max(ic - 1, 0), i1 = min(ic, a.C - 1);
             const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
             const float *pv = pb + (size_t)v * pview;
+            const float4 *qv = QUAD ? pq + (size_t)v * (a.n_rows + 1) * (a.C + 1) + ic : pq;
             // row + 1/2 of slice k0 + kk: rr0 + kk * drr
             const float slope = a.row_scale * rU;
             const float zs = view_z ? __ldg(view_z + v) : 0.0f;
@@ -132,10 +146,21 @@ __global__ void __launch_bounds__(kThreads)
                 int ir;
                 float fr;
                 split_pos(rr, ir, fr);
-                const int r0 = min(max(ir - 1, 0), a.n_rows - 1), r1 = min(ir, a.n_rows - 1);
-                const float *ra = pv + (size_t)r0 * a.C, *rc = pv + (size_t)r1 * a.C;
-                const float va0 = __ldg(ra + i0), va1 = __ldg(ra + i1);
-                const float vc0 = __ldg(rc + i0), vc1 = __ldg(rc + i1);
+                float va0, va1, vc0, vc1;
+                if constexpr (QUAD) {
+                    const float4 t = __ldg(qv + (size_t)ir * (a.C + 1));
+                    va0 = t.x;
+                    va1 = t.y;
+                    vc0 = t.z;
+                    vc1 = t.w;
+                } else {
+                    const int r0 = min(max(ir - 1, 0), a.n_rows - 1), r1 = min(ir, a.n_rows - 1);
+                    const float *ra = pv + (size_t)r0 * a.C, *rc = pv + (size_t)r1 * a.C;
+                    va0 = __ldg(ra + i0);
+                    va1 = __ldg(ra + i1);
+                    vc0 = __ldg(rc + i0);
+                    vc1 = __ldg(rc + i1);
+                }
                 if constexpr (TEX) {
                     const float4 w = tex_weights2d(A, floorf(fmaf(fr, 256.0f, 0.5f)));
                     const float val = fmaf(w.x, va0, fmaf(w.y, va1, fmaf(w.z, vc0, w.w * vc1)));
@@ -153,6 +178,24 @@ __global__ void __launch_bounds__(kThreads)
         for (int kk = 0; kk < ZC; ++kk)
             if (k0 + kk < a.nz) vb[((size_t)(k0 + kk) * a.ny + iy) * a.nx + ix] = acc[kk];
     }
+}
+
+// Quad images of the views of one volume: [V][n_rows+1][C+1] float4, cell
+// (ir, ic) = taps (r0, i0), (r0, i1), (r1, i0), (r1, i1) with
+// r0 = min(max(ir-1, 0), n_rows-1), r1 = min(ir, n_rows-1), i0 = max(ic-1, 0),
+// i1 = min(ic, C-1): cone_bp_kernel's clamped taps for row and column
+// positions ir in [0, n_rows] and ic in [0, C].
+__global__ void __launch_bounds__(256)
+    cone_proj_quads_kernel(const float *__restrict__ proj, float4 *__restrict__ pq, int R,
+                           int C) {
+    const int ic = blockIdx.x * 256 + threadIdx.x, ir = blockIdx.y, v = blockIdx.z;
+    if (ic > C) return;
+    const int i0 = max(ic - 1, 0), i1 = min(ic, C - 1);
+    const int r0 = min(max(ir - 1, 0), R - 1), r1 = min(ir, R - 1);
+    const float *pv = proj + (size_t)v * R * C;
+    const float *ra = pv + (size_t)r0 * C, *rc = pv + (size_t)r1 * C;
+    pq[((size_t)v * (R + 1) + ir) * (C + 1) + ic] =
+        make_float4(__ldg(ra + i0), __ldg(ra + i1), __ldg(rc + i0), __ldg(rc + i1));
 }
 
 // ---- CB_EA transpose ---------------------------------------------------------
@@ -845,22 +888,54 @@ ConeArgs make_cone_args(const ct_plan *p) {
 
 }  // namespace
 
-int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream) {
+size_t cone_bp_work_bytes(const ct_plan *p) {
+    // one volume's quad images, where they stay within 4 GB
+    const size_t q = sizeof(float4) * (size_t)p->g.n_views * (p->n_rows + 1) * (p->g.n_cols + 1);
+    return q <= ((size_t)4 << 30) ? q : 0;
+}
+
+int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *work,
+            void *stream) {
     const ConeArgs a = make_cone_args(p);
     constexpr int ZC = kZC;
     const int zgroups = (a.nz + ZC - 1) / ZC;
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool tex = p->opts.texture_weights != 0;
+    const size_t per_proj = (size_t)a.V * a.n_rows * a.C, per_vol = (size_t)a.nz * a.ny * a.nx;
+    if (work && cone_bp_work_bytes(p)) {
+        float4 *pq = static_cast<float4 *>(work);
+        auto kern = a.atan_deg == 4
+                        ? (tex ? cone_bp_kernel<ZC, 4, true, true> : cone_bp_kernel<ZC, 4, false, true>)
+                    : a.atan_deg == 8
+                        ? (tex ? cone_bp_kernel<ZC, 8, true, true> : cone_bp_kernel<ZC, 8, false, true>)
+                        : (tex ? cone_bp_kernel<ZC, 0, true, true> : cone_bp_kernel<ZC, 0, false, true>);
+        for (int b = 0; b < batch; ++b) {
+            const float *pp = proj + (size_t)b * per_proj;
+            for (int v0 = 0; v0 < a.V; v0 += 65535) {
+                const int nv = a.V - v0 < 65535 ? a.V - v0 : 65535;
+                cone_proj_quads_kernel<<<dim3((a.C + 1 + 255) / 256, a.n_rows + 1, nv), 256, 0,
+                                         s>>>(pp + (size_t)v0 * a.n_rows * a.C,
+                                              pq + (size_t)v0 * (a.n_rows + 1) * (a.C + 1),
+                                              a.n_rows, a.C);
+                ct_count_launch();
+            }
+            kern<<<dim3((a.nx + 31) / 32, (a.ny + 7) / 8, zgroups), dim3(32, 8), 0, s>>>(
+                pp, pq, vol + (size_t)b * per_vol, vcs, p->d_view_z, a, 1);
+            ct_count_launch();
+        }
+        return (int)cudaGetLastError();
+    }
+    auto kern = a.atan_deg == 4
+                    ? (tex ? cone_bp_kernel<ZC, 4, true, false> : cone_bp_kernel<ZC, 4, false, false>)
+                : a.atan_deg == 8
+                    ? (tex ? cone_bp_kernel<ZC, 8, true, false> : cone_bp_kernel<ZC, 8, false, false>)
+                    : (tex ? cone_bp_kernel<ZC, 0, true, false> : cone_bp_kernel<ZC, 0, false, false>);
     for (int b0 = 0; b0 < batch; b0 += 4096) {
         const int nb = batch - b0 < 4096 ? batch - b0 : 4096;
         dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, zgroups * nb);
-        const float *pp = proj + (size_t)b0 * a.V * a.n_rows * a.C;
-        float *vp = vol + (size_t)b0 * a.nz * a.ny * a.nx;
-        cudaStream_t s = (cudaStream_t)stream;
-        const bool tex = p->opts.texture_weights != 0;
-        auto kern = a.atan_deg == 4   ? (tex ? cone_bp_kernel<ZC, 4, true> : cone_bp_kernel<ZC, 4, false>)
-                    : a.atan_deg == 8 ? (tex ? cone_bp_kernel<ZC, 8, true> : cone_bp_kernel<ZC, 8, false>)
-                                      : (tex ? cone_bp_kernel<ZC, 0, true> : cone_bp_kernel<ZC, 0, false>);
-        kern<<<grid, dim3(32, 8), 0, s>>>(pp, vp, vcs, p->d_view_z, a, nb);
+        kern<<<grid, dim3(32, 8), 0, s>>>(proj + (size_t)b0 * per_proj, nullptr,
+                                          vol + (size_t)b0 * per_vol, vcs, p->d_view_z, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();

@@ -110,7 +110,11 @@ inline bool has_preweight(const ct_plan *p) { return p->d_parker || p->d_cosw; }
 // out = in * parker[v][c] * cosw[r][c] (each factor when present), over
 // [batch][V][n_rows][C]
 int apply_preweight(const ct_plan *p, const float *in, float *out, int batch, void *stream);
-int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *stream);
+// work: cone_bp_work_bytes(p) bytes (one volume's quad images of the views;
+// 0 where they would not fit in 4 GB) or NULL (four gathers per sample)
+size_t cone_bp_work_bytes(const ct_plan *p);
+int cone_bp(const ct_plan *p, const float *proj, float *vol, int batch, void *work,
+            void *stream);
 // work: cone_bp_transpose_work_bytes(p, batch) bytes (per-volume max |vol|;
 // where every detector row of a view fits in shared memory, also pixel tables
 // and a z-major copy of the volumes)

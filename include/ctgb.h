@@ -292,7 +292,9 @@ ct_status ct_plan_create_cone_ex(const ct_fan_geom *geom, int n_rows, int nz,
 /* The reference's CB_EA backprojection (FDK/GPURecon_GPU.cu:15-50) over all
  * views, unfiltered: per voxel in the FOV disc and view, the bilinear
  * (col, row) sample of the view with col as in ct_bp_fan and
- * row = (z*D/U - det_bottom)/drow (clamped rows), times 1/(U^2+t^2). */
+ * row = (z*D/U - det_bottom)/drow (clamped rows), times 1/(U^2+t^2).
+ * Allocates its scratch (one volume's tap images, 16 B per detector cell)
+ * stream-ordered on `stream`. */
 ct_status ct_cone_bp(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,
                      ct_stream stream);
 
