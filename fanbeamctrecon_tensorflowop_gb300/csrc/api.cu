@@ -87,6 +87,13 @@ size_t proj_bytes(const ct_plan *p, int batch) {
     return sizeof(float) * (size_t)batch * p->g.n_views * p->n_rows * p->g.n_cols;
 }
 
+// where FBP's backprojection work starts (after its sinogram copies,
+// 256-byte aligned)
+size_t fbp_work_offset(const ct_plan *p, int batch) {
+    const size_t copies = ctk::has_preweight(p) ? 2 : 1;
+    return (copies * sino_bytes(p, batch) + 255) & ~(size_t)255;
+}
+
 // where FDK's backprojection work starts (after its projection copies,
 // 256-byte aligned)
 size_t fdk_cone_work_offset(const ct_plan *p, int batch) {
@@ -114,9 +121,10 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
             return ctk::fp_fan_work_bytes(p, batch);
         case CT_OP_FP_ADJOINT:
             return ctk::fp_fan_adjoint_work_bytes(p, batch);
-        case CT_OP_FBP:
-        case CT_OP_FBP_ADJOINT:
+        case CT_OP_FBP:  // + the backprojection's tap images
         case CT_OP_FDK_BP:
+            return fbp_work_offset(p, batch) + ctk::bp_fan_work_bytes(p, batch);
+        case CT_OP_FBP_ADJOINT:
             return parker * sino_bytes(p, batch);
         default:
             return 0;
@@ -166,7 +174,10 @@ ct_status filtered_bp(const ct_plan *p, const float *d_sino, float *d_img, int b
     }
     st = launch_status(ctk::ramp_filter(p, src, filt, batch * p->g.n_views, s), name);
     if (st != CT_OK) return st;
-    return launch_status(ctk::bp_fan(p, filt, d_img, batch, 1, s), name);
+    void *bwork = ctk::bp_fan_work_bytes(p, batch)
+                      ? static_cast<char *>(w.ptr) + fbp_work_offset(p, batch)
+                      : nullptr;
+    return launch_status(ctk::bp_fan(p, filt, d_img, batch, 1, bwork, s), name);
 }
 
 }  // namespace
@@ -428,7 +439,10 @@ ct_status ct_bp_fan(const ct_plan *plan, const float *d_sino, float *d_img, int 
     if (st != CT_OK || batch == 0) return st;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
-    return launch_status(ctk::bp_fan(plan, d_sino, d_img, batch, 0, stream), "ct_bp_fan");
+    Workspace w;
+    st = acquire(w, nullptr, 0, ctk::bp_fan_work_bytes(plan, batch), stream);
+    if (st != CT_OK) return st;
+    return launch_status(ctk::bp_fan(plan, d_sino, d_img, batch, 0, w.ptr, stream), "ct_bp_fan");
 }
 
 ct_status ct_bp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_sino, int batch,

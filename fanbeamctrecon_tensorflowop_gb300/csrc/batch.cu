@@ -289,6 +289,14 @@ struct Layout {
 };
 constexpr size_t kCounterBytes = 256;
 
+// Where an FBP slice group's tap images start in its workspace (after the
+// filtered and pre-weighted sinograms, 256-byte aligned).
+size_t group_pairs_offset(const ct_batch_item &it, int g) {
+    const ct_plan *p = it.plan;
+    const size_t sino = sizeof(float) * (size_t)g * p->g.n_views * p->g.n_cols;
+    return ((has_preweight(p) ? 2 : 1) * sino + 255) & ~(size_t)255;
+}
+
 // Workspace of a slice group's plan path.
 size_t group_work_bytes(const ct_batch_item &it, int g) {
     const ct_plan *p = it.plan;
@@ -296,7 +304,10 @@ size_t group_work_bytes(const ct_batch_item &it, int g) {
     switch (it.op) {
         case CT_OP_FP:
             return fp_fan_work_bytes(p, g);
-        case CT_OP_FBP:  // filtered (+ pre-weighted) sinograms
+        case CT_OP_BP:  // tap images
+            return bp_fan_work_bytes(p, g);
+        case CT_OP_FBP:  // filtered (+ pre-weighted) sinograms, then tap images
+            return group_pairs_offset(it, g) + bp_fan_work_bytes(p, g);
         case CT_OP_FBP_ADJOINT:  // transposed (+ filtered) sinograms
             return (has_preweight(p) ? 2 : 1) * sino;
         default:
@@ -470,14 +481,18 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
             if (f.op == CT_OP_FP) {
                 r = fp_fan(p, in, out, g, wk, s);
             } else if (f.op == CT_OP_BP) {
-                r = bp_fan(p, in, out, g, 0, s);
+                r = bp_fan(p, in, out, g, 0, bp_fan_work_bytes(p, g) ? wk : nullptr, s);
             } else if (f.op == CT_OP_FBP) {  // as ct_fbp_fan
                 const float *src = in;
                 if (has_preweight(p)) {
                     if ((r = apply_preweight(p, in, wk + sino, g, s)) == 0) src = wk + sino;
                 }
                 if (r == 0) r = ramp_filter(p, src, wk, rows, s);
-                if (r == 0) r = bp_fan(p, wk, out, g, 1, s);
+                void *pw = bp_fan_work_bytes(p, g)
+                               ? static_cast<char *>(static_cast<void *>(wk)) +
+                                     group_pairs_offset(f, g)
+                               : nullptr;
+                if (r == 0) r = bp_fan(p, wk, out, g, 1, pw, s);
             } else {  // CT_OP_FBP_ADJOINT, as ct_fbp_fan_adjoint
                 r = bp_fan_transpose(p, in, wk, g, 1, s);
                 if (r == 0 && !has_preweight(p)) {

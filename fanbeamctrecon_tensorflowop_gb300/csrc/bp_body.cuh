@@ -56,13 +56,18 @@ __device__ __forceinline__ float tex_weight(float f) {
 // sino + s * sstride ([V][C]), image slice s at img + s * istride ([ny][nx]).
 // Block of 32 x 8 threads, ROWS pixels per thread (32 x 32 tiles by default);
 // block-uniform call.  TEX: texture-unit weights (tex_weight) instead of
-// exact FP32 ones.
+// exact FP32 ones.  PAIRS (SB = 4): the taps come from the slice group's tap
+// image `pairs` ([V][C+1] x 2 float4: for column position i, the clamped taps
+// (i0, i1) of slices 0..3), two 16-byte loads per pixel-view for the four
+// slices instead of eight 4-byte gathers; same values, same arithmetic.
 template <bool WEIGHTED, int SB, int DEG, typename OutT, int ROWS = kBpRowsPerThr,
-          bool TEX = false>
+          bool TEX = false, bool PAIRS = false>
 __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t sstride,
                                         OutT *__restrict__ img, size_t istride,
                                         const float2 *__restrict__ view_cs, const BpArgs &a,
-                                        int nsl, int tx, int ty) {
+                                        int nsl, int tx, int ty,
+                                        const float4 *__restrict__ pairs = nullptr) {
+    static_assert(!PAIRS || SB == 4, "tap images hold four slices");
     const int ix = tx * kBpTile + threadIdx.x;
     const int iy0 = ty * (8 * ROWS) + threadIdx.y;
     float py[ROWS];
@@ -105,10 +110,22 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
                     const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
                     float wgt = 1.0f;
                     if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));
+                    float v0[SB], v1[SB];
+                    if constexpr (PAIRS) {
+                        const float4 *q = pairs + ((size_t)v * (a.C + 1) + i) * 2;
+                        const float4 t0 = __ldg(q), t1 = __ldg(q + 1);
+                        v0[0] = t0.x, v1[0] = t0.y, v0[1] = t0.z, v1[1] = t0.w;
+                        v0[2] = t1.x, v1[2] = t1.y, v0[3] = t1.z, v1[3] = t1.w;
+                    } else {
+#pragma unroll
+                        for (int s = 0; s < SB; ++s) {
+                            v0[s] = __ldg(sb[s] + ro + i0);
+                            v1[s] = __ldg(sb[s] + ro + i1);
+                        }
+                    }
 #pragma unroll
                     for (int s = 0; s < SB; ++s) {
-                        const float v0 = __ldg(sb[s] + ro + i0), v1 = __ldg(sb[s] + ro + i1);
-                        const float val = fmaf(f, v1 - v0, v0);
+                        const float val = fmaf(f, v1[s] - v0[s], v0[s]);
                         acc[s][k] = WEIGHTED ? fmaf(val, wgt, acc[s][k]) : acc[s][k] + val;
                     }
                 }

@@ -93,7 +93,11 @@ int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, v
                    void *stream);
 
 // mode 0: unweighted BP, 1: 1/(U^2+t^2)-weighted (FBP / FDK 2-D)
-int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weighted, void *stream);
+// work: bp_fan_work_bytes(p, batch) bytes (tap images of up to 16 slice groups
+// of four; 0 below four slices) or NULL (gathers)
+size_t bp_fan_work_bytes(const ct_plan *p, int batch);
+int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weighted, void *work,
+           void *stream);
 int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch, int weighted,
                      void *stream);
 int ramp_filter(const ct_plan *p, const float *in, float *out, int rows, void *stream);

@@ -92,7 +92,7 @@ extern "C" ct_status ct_fbp_fan_static_scratch(const ct_plan *plan, const float 
     // backprojection reads them, so nothing left by an earlier call is used.
     e = (cudaError_t)ctk::ramp_filter(plan, d_sino, scratch, batch * plan->g.n_views, stream);
     if (e != cudaSuccess) return fail_cuda(e, "ct_fbp_fan_static_scratch (filter)");
-    e = (cudaError_t)ctk::bp_fan(plan, scratch, d_img, batch, 1, stream);
+    e = (cudaError_t)ctk::bp_fan(plan, scratch, d_img, batch, 1, nullptr, stream);
     if (e != cudaSuccess) return fail_cuda(e, "ct_fbp_fan_static_scratch (backprojection)");
     return CT_OK;
 }
