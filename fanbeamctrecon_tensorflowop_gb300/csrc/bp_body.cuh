@@ -56,10 +56,10 @@ __device__ __forceinline__ float tex_weight(float f) {
 // sino + s * sstride ([V][C]), image slice s at img + s * istride ([ny][nx]).
 // Block of 32 x 8 threads, ROWS pixels per thread (32 x 32 tiles by default);
 // block-uniform call.  TEX: texture-unit weights (tex_weight) instead of
-// exact FP32 ones.  PAIRS (SB = 4): the taps come from the slice group's tap
-// image `pairs` ([V][C+1] x 2 float4: for column position i, the clamped taps
-// (i0, i1) of slices 0..3), two 16-byte loads per pixel-view for the four
-// slices instead of eight 4-byte gathers; same values, same arithmetic.
+// exact FP32 ones.  PAIRS (SB = 4 or 8): the taps come from the slice group's
+// tap image `pairs` ([V][C+1] x SB/2 float4: for column position i, the
+// clamped taps (i0, i1) of slices 0..SB-1), SB/2 16-byte loads per pixel-view
+// instead of 2 SB 4-byte gathers; same values, same arithmetic.
 template <bool WEIGHTED, int SB, int DEG, typename OutT, int ROWS = kBpRowsPerThr,
           bool TEX = false, bool PAIRS = false>
 __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t sstride,
@@ -67,7 +67,7 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
                                         const float2 *__restrict__ view_cs, const BpArgs &a,
                                         int nsl, int tx, int ty,
                                         const float4 *__restrict__ pairs = nullptr) {
-    static_assert(!PAIRS || SB == 4, "tap images hold four slices");
+    static_assert(!PAIRS || SB == 4 || SB == 8, "tap images hold four or eight slices");
     const int ix = tx * kBpTile + threadIdx.x;
     const int iy0 = ty * (8 * ROWS) + threadIdx.y;
     float py[ROWS];
@@ -112,10 +112,13 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
                     if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));
                     float v0[SB], v1[SB];
                     if constexpr (PAIRS) {
-                        const float4 *q = pairs + ((size_t)v * (a.C + 1) + i) * 2;
-                        const float4 t0 = __ldg(q), t1 = __ldg(q + 1);
-                        v0[0] = t0.x, v1[0] = t0.y, v0[1] = t0.z, v1[1] = t0.w;
-                        v0[2] = t1.x, v1[2] = t1.y, v0[3] = t1.z, v1[3] = t1.w;
+                        const float4 *q = pairs + ((size_t)v * (a.C + 1) + i) * (SB / 2);
+#pragma unroll
+                        for (int h = 0; h < SB / 2; ++h) {
+                            const float4 t = __ldg(q + h);
+                            v0[2 * h] = t.x, v1[2 * h] = t.y, v0[2 * h + 1] = t.z,
+                                     v1[2 * h + 1] = t.w;
+                        }
                     } else {
 #pragma unroll
                         for (int s = 0; s < SB; ++s) {
