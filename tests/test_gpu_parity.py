@@ -107,6 +107,36 @@ def test_bp_and_adjoint(case, cuda, orc):
         assert rel_l2(got_t[1], _np(plan.bp_adjoint(_t(x[1:2], cuda)))[0]) <= 1e-6
 
 
+@pytest.mark.parametrize("nb", [16, 40])
+def test_transpose_slice_groups(case, cuda, orc, nb):
+    """Batches of 16 and 40 slices through the BP / FBP transposes (four
+    slices per thread, 40: ten groups).  Three slices against the oracle,
+    each also against the one-slice path."""
+    name, p, a, plan, _, g = case
+    x = _images(g, nb, seed=9)
+    pick = [0, nb // 2, nb - 1]
+    for fn, oref in ((plan.bp_adjoint, orc.bp_fan_transpose),
+                     (plan.fbp_adjoint, orc.fbp_fan_adjoint)):
+        got = _np(fn(_t(x, cuda)))
+        ref = oref(g, a, x[pick])
+        assert rel_l2(got[pick], ref) <= TOL, (nb, rel_l2(got[pick], ref))
+        for k in pick:
+            alone = _np(fn(_t(x[k:k + 1], cuda)))[0]
+            assert rel_l2(got[k], alone) <= 1e-5, (k, rel_l2(got[k], alone))
+
+
+def test_transpose_slice_groups_dot(case, cuda):
+    name, p, a, plan, _, g = case
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal((16, g.ny, g.nx)).astype(np.float32)
+    y = rng.standard_normal((16, g.n_views, g.n_cols)).astype(np.float32)
+    xt, yt = _t(x, cuda), _t(y, cuda)
+    for k, (ax, aty) in {"bp": (plan.bp_adjoint(xt), plan.bp(yt)),
+                         "fbp": (plan.fbp_adjoint(xt), plan.fbp(yt))}.items():
+        m = _dot_mismatch(_np(ax), y.astype(np.float64), x.astype(np.float64), _np(aty))
+        assert m <= DOT_TOL, (k, m)
+
+
 @pytest.mark.parametrize("window", ["ramlak", "shepp_logan"])
 def test_ramp_filter(case, cuda, orc, window):
     name, p, a, plan, plan_sl, g = case

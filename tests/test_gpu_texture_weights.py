@@ -98,6 +98,28 @@ def test_texture_mode_against_oracle_and_adjoints(cuda, texture_oracle):
         assert m <= DOT_TOL, m
 
 
+def test_texture_mode_transpose_slice_groups(cuda, texture_oracle):
+    """The BP transpose of 16 slices with the texture weights: two slices
+    against the emulating oracle, dot test."""
+    orc = texture_oracle
+    p, a = G.small(n=50, ny=38, shift=1.5, views=72, cols=100)
+    g = orc.decode(p)
+    plan = FanPlan(p, a, device=cuda, texture_weights=True)
+    x = np.stack([phantom.ellipse_phantom(g.nx, float(g.dx), seed=s, ny=g.ny)
+                  for s in range(16)]).astype(np.float32)
+    got = _np(plan.bp_adjoint(_t(x, cuda)))
+    e = rel_l2(got[[0, 15]], orc.bp_fan_transpose(g, a, x[[0, 15]]))
+    assert e <= TOL, e
+    rng = np.random.default_rng(5)
+    xx = rng.standard_normal((16, g.ny, g.nx)).astype(np.float32)
+    yy = rng.standard_normal((16, g.n_views, g.n_cols)).astype(np.float32)
+    ax = _np(plan.bp_adjoint(_t(xx, cuda)))
+    aty = _np(plan.bp(_t(yy, cuda)))
+    m = abs(float(np.vdot(ax, yy)) - float(np.vdot(xx, aty))) / (
+        np.linalg.norm(ax) * np.linalg.norm(yy))
+    assert m <= DOT_TOL, m
+
+
 def test_texture_mode_cone(cuda, texture_oracle):
     orc = texture_oracle
     p, a, nr, nz = G.cone_small()
