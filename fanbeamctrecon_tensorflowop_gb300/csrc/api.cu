@@ -529,10 +529,8 @@ ct_status ct_cone_bp(const ct_plan *plan, const float *d_proj, float *d_vol, int
     if (st != CT_OK || batch == 0) return st;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
-    Workspace w;
-    st = acquire(w, nullptr, 0, ctk::cone_bp_work_bytes(plan), stream);
-    if (st != CT_OK) return st;
-    return launch_status(ctk::cone_bp(plan, d_proj, d_vol, batch, w.ptr, stream), "ct_cone_bp");
+    // no scratch: four gathers per sample (FDK's tap images need a workspace)
+    return launch_status(ctk::cone_bp(plan, d_proj, d_vol, batch, nullptr, stream), "ct_cone_bp");
 }
 
 ct_status ct_fdk_cone(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,

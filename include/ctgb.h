@@ -293,8 +293,8 @@ ct_status ct_plan_create_cone_ex(const ct_fan_geom *geom, int n_rows, int nz,
  * views, unfiltered: per voxel in the FOV disc and view, the bilinear
  * (col, row) sample of the view with col as in ct_bp_fan and
  * row = (z*D/U - det_bottom)/drow (clamped rows), times 1/(U^2+t^2).
- * Allocates its scratch (one volume's tap images, 16 B per detector cell)
- * stream-ordered on `stream`. */
+ * Needs no scratch: it gathers the four taps of each sample from d_proj
+ * (ct_fdk_cone reads them from per-view tap images in its workspace). */
 ct_status ct_cone_bp(const ct_plan *plan, const float *d_proj, float *d_vol, int batch,
                      ct_stream stream);
 
