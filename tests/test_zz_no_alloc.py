@@ -24,11 +24,13 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4  # relative L2, as in test_gpu_parity.py
 
 
-def test_static_scratch_fbp_matches_fbp(cuda):
+@pytest.mark.parametrize("B", [3, 6])
+def test_static_scratch_fbp_matches_fbp(cuda, B):
+    """3 slices: one per thread; 6: four per thread with a ragged group, read by
+    gathers here and from tap images by ct_fbp_fan (the same values)."""
     p, a = G.config0()  # 256^2, 720 views x 512 channels
     plan = FanPlan(p, a, device=cuda)
     lib = _lib.load()
-    B = 3
     gen = torch.Generator(device=cuda).manual_seed(0)
     stream = torch.cuda.current_stream(cuda).cuda_stream
     outs = []
