@@ -265,9 +265,18 @@ int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weigh
             float *ip = img + (size_t)b0 * plane;
             bp_pairs_kernel<4><<<dim3((a.C + 1 + 255) / 256, a.V, groups), 256, 0, s>>>(
                 sp, pairs, a.V, a.C, nb);
-            dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + kTile - 1) / kTile, groups);
-            launch_bp_any<4, true>(weighted != 0, tex, p->atan_deg, grid, s, sp, pairs, ip, vcs,
-                                   a, nb);
+            // pixel rows per thread (tiles of 32 x 8 rows): 2 for BP, 1 for the
+            // weighted form (32 clinical slices: BP 4.10 / 3.64 / 3.73 ms with 4 / 2 / 1
+            // rows, FBP 4.94 / 4.29 / 4.21 ms); fewer rows, fewer registers, more blocks
+            if (weighted) {
+                dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 7) / 8, groups);
+                launch_bp_any<4, true, 1>(true, tex, p->atan_deg, grid, s, sp, pairs, ip, vcs,
+                                          a, nb);
+            } else {
+                dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 15) / 16, groups);
+                launch_bp_any<4, true, 2>(false, tex, p->atan_deg, grid, s, sp, pairs, ip, vcs,
+                                          a, nb);
+            }
             ct_count_launch(2);
         }
         return (int)cudaGetLastError();
