@@ -432,6 +432,30 @@ __global__ void __launch_bounds__(32)
     }
 }
 
+// Column pairs (i0, i1) in one 64-bit register for the f32x2 instructions
+// (each lane rounds as the FP32 instruction does; 27.35 -> 26.80 ms per
+// clinical FDK adjoint against the scalar form).
+__device__ __forceinline__ unsigned long long zt_pack(float x, float y) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+    return r;
+}
+__device__ __forceinline__ float2 zt_unpack(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ unsigned long long zt_mul2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long zt_add2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // A warp's pixels: image rows in order, in each the tiles of `per` pixels
 // t = (warp + iy) mod NW + NW m of the row's FOV span [x0, end).
 struct ZtCursor {
@@ -518,10 +542,12 @@ __global__ void __launch_bounds__(kZThreads, 1)
                 const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
                 const float slope = a.row_scale * rU;
                 const float drr = a.dz * slope;
-                auto emit = [&](int row, float x0, float x1) {
+                const unsigned long long g01 = zt_pack(1.0f - f, f);  // column weights
+                auto emit = [&](int row, unsigned long long X) {
                     const float sc = (unsigned)(row - 1) < (unsigned)(last - 1) ? scale : scale_c;
-                    atomicAdd(c0 + row, __float2int_rn(x0 * sc));
-                    atomicAdd(c1 + row, __float2int_rn(x1 * sc));
+                    const float2 v = zt_unpack(zt_mul2(X, zt_pack(sc, sc)));
+                    atomicAdd(c0 + row, __float2int_rn(v.x));
+                    atomicAdd(c1 + row, __float2int_rn(v.y));
                 };
                 // passes of gp groups (one pass unless nz > 32 * kZS)
                 for (int kb = g * kZS; kb < a.nz; kb += gp * kZS) {
@@ -540,8 +566,9 @@ __global__ void __launch_bounds__(kZThreads, 1)
                     const int kg = kb & ~(kZC - 1);
                     const float rr0 = fmaf(group_z(a, kg) - zs, slope, a.row_off);
                     const float kk0 = (float)(kb - kg);
-                    int prow = -1;  // the pending row and its two column sums
-                    float p0 = 0.0f, p1 = 0.0f;
+                    // the pending row and its column pair (i0, i1), packed for f32x2
+                    int prow = -1;
+                    unsigned long long P = 0ull;
 #pragma unroll
                     for (int j = 0; j < kZS; ++j) {
                         // (slices beyond nz read zero and add nothing)
@@ -552,35 +579,30 @@ __global__ void __launch_bounds__(kZThreads, 1)
                         split_pos(rr, ir, fr);
                         const int lo = min(max(ir - 1, 0), last), hi = min(ir, last);
                         const float vw = x[j] * wgt;
-                        float l0, l1, h0, h1;  // (lo, i0), (lo, i1), (hi, i0), (hi, i1)
+                        unsigned long long L, H;  // rows lo and hi, columns (i0, i1)
                         if constexpr (TEX) {
                             const float4 w = tex_weights2d(A, floorf(fmaf(fr, 256.0f, 0.5f)));
-                            const float s = vw * (1.0f / 256.0f);
-                            l0 = s * w.x;
-                            l1 = s * w.y;
-                            h0 = s * w.z;
-                            h1 = s * w.w;
+                            const float sw = vw * (1.0f / 256.0f);
+                            const unsigned long long ss = zt_pack(sw, sw);
+                            L = zt_mul2(ss, zt_pack(w.x, w.y));
+                            H = zt_mul2(ss, zt_pack(w.z, w.w));
                         } else {
                             const float hb = vw * fr, lb = vw - hb;
-                            l0 = lb * (1.0f - f);
-                            l1 = lb * f;
-                            h0 = hb * (1.0f - f);
-                            h1 = hb * f;
+                            L = zt_mul2(zt_pack(lb, lb), g01);
+                            H = zt_mul2(zt_pack(hb, hb), g01);
                         }
                         const bool flush = prow != lo;
-                        if (flush && prow >= 0) emit(prow, p0, p1);
-                        const float q0 = flush ? l0 : p0 + l0, q1 = flush ? l1 : p1 + l1;
+                        if (flush && prow >= 0) emit(prow, P);
+                        const unsigned long long Q = flush ? L : zt_add2(P, L);
                         if (hi == lo) {  // both row taps on one row (clamped): keep it
-                            p0 = q0 + h0;
-                            p1 = q1 + h1;
+                            P = zt_add2(Q, H);
                         } else {
-                            emit(lo, q0, q1);
-                            p0 = h0;
-                            p1 = h1;
+                            emit(lo, Q);
+                            P = H;
                         }
                         prow = hi;
                     }
-                    emit(prow, p0, p1);
+                    emit(prow, P);
                 }
             }
         }
