@@ -87,8 +87,9 @@ def test_fdk_adjoint(cone, cuda, orc):
 
 
 TRANSPOSE_CASES = {
-    # 45 slices (two 32-slice chunks of the lanes-along-z kernel) on a detector
-    # a third as tall as the magnified volume: samples clamp onto both edge rows
+    # 45 slices (six 8-slice lane groups, the last one ragged, in the
+    # lanes-along-z kernel) on a detector a third as tall as the magnified
+    # volume: samples clamp onto both edge rows
     "tall_clamped": lambda: G.cone_small(n=30, views=40, cols=60, n_rows=20, nz=45, pixel=6.0,
                                          dz=2.0, drow=3.0),
     # more detector rows than one view's accumulators fit in shared memory:
@@ -173,3 +174,32 @@ def test_fdk_adjoint_high_dynamic_range(cuda, orc):
     assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
     zero = plan.fdk_adjoint(torch.zeros((1, nz, g.ny, g.nx), device=cuda))
     assert float(zero.abs().max()) == 0.0
+
+
+def test_cone_full_size_properties(cuda):
+    """At the clinical cone size (512^2 x 64 voxels, 984 views of 888 x 64),
+    properties that need no oracle: linearity of FDK and of the cone FP, the
+    FDK adjoint's dot test, and that a volume in a batch equals the volume
+    alone (tap images, fixed-point scale and quad images are per volume)."""
+    p, a, nr, nz = G.config4()
+    plan = ConePlan(p, a, nr, nz, device=cuda)
+    gen = torch.Generator(device=cuda).manual_seed(0)
+    y1 = torch.rand((2, *plan.proj_shape), device=cuda, generator=gen)
+    y2 = torch.rand((2, *plan.proj_shape), device=cuda, generator=gen)
+    f1, f2 = plan.fdk(y1), plan.fdk(y2)
+    assert rel_l2(_np(plan.fdk(2.0 * y1 - 3.0 * y2)), _np(2.0 * f1 - 3.0 * f2)) < 1e-5
+    assert torch.equal(plan.fdk(y1[1:2])[0], f1[1])
+    x = torch.randn((2, *plan.volume_shape), device=cuda, generator=gen)
+    yy = torch.randn((2, *plan.proj_shape), device=cuda, generator=gen)
+    ax = plan.fdk_adjoint(x)
+    aty = plan.fdk(yy)
+    m = abs(float(torch.vdot(ax.double().flatten(), yy.double().flatten())) -
+            float(torch.vdot(x.double().flatten(), aty.double().flatten()))) / (
+        float(ax.double().norm()) * float(yy.double().norm()))
+    assert m <= DOT_TOL, m
+    assert torch.equal(plan.fdk_adjoint(x[1:2])[0], ax[1])
+    v1 = torch.rand((2, *plan.volume_shape), device=cuda, generator=gen)
+    p1 = plan.fp_cone(v1)
+    p2 = plan.fp_cone(v1[1:2])
+    assert torch.equal(p2[0], p1[1])
+    assert rel_l2(_np(plan.fp_cone(3.0 * v1)), 3.0 * _np(p1)) < 1e-6
