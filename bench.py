@@ -9,14 +9,23 @@ Inputs rotate over 4 batches (576 MB of images + sinograms, > the 129 MB L2).
 Also reported: ``e2e`` (the same FP through the reference-named Python entry
 point ``utils.fp_fan_curve`` with host numpy buffers, host<->device copies
 inside the timed region), BP throughput (G pixel-views/s, U[0,1)
-sinograms), Shepp-Logan FBP time, and the batch-32 FP + adjoint step against
-the plain per-view launch loop on the same GPU.
+sinograms), Shepp-Logan FBP time, the batch-32 FP + adjoint step against the
+plain per-view launch loop on the same GPU, cone beam and uneven batches.
 
-``--impl reference`` times the reference algorithm on the host CPU (the FP64
-oracle restatement, all cores).  The reference's ops cannot be built for the
-GPU, and their host-compiled form (oracle/build_ref.py, which runs each CUDA
-thread as a fiber) exists only where the reference's sources are and is no
-measure of its speed.
+Roofline: the interpolation kernels are bound by the L1 data path (their
+gathers hit L1), so ``roofline`` sets the forward projector's algorithmic L1
+load bytes -- one 16-byte quad per (ray, cell) visit and slice -- against the
+L1 load peak that ``csrc/peaks`` measures in this same run; the compulsory
+and the measured DRAM traffic are reported beside it.
+
+``cpu_baseline`` and ``--impl reference`` time the reference's algorithms on
+the host cores as an FP32 OpenMP transcription (oracle/cpu_fp32.c).  The
+reference's ops cannot be built for the GPU (CUDA 13 rejects texture
+references; TensorFlow and IPP are absent).  The same leg checks every
+output against the FP64 oracle (``errors``), outside all timed regions.
+
+``--profile-case OP`` runs one operator a few times for a profiler (see
+``profile_case``).
 
 Multi-GPU: ``torchrun --nproc-per-node N bench.py --gpus N``: every rank runs
 its own batch (replicas, no collective on the data path); the step time is
@@ -25,8 +34,8 @@ the max over ranks and ``value`` counts the rays of all ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -49,10 +58,10 @@ BATCH = 32
 POOL = 4
 WORKLOAD = ("fan-beam FP, batch of 32 seeded ellipse phantoms 512x512 @0.7 mm, "
             "984 views x 888 equiangular channels (1 mm pitch), SID 541 / SDD 949 mm")
-GATHER_BYTES_PER_SAMPLE = 16  # four FP32 bilinear taps per ray sample
-FLOP_PER_SAMPLE = 16          # 2 FMA position, 2 fractions, 3 lerps, 1 add (FMA = 2)
-# FP32 FMA peak, derived: 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz (max SM clock)
-FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
+QUAD_BYTES = 16      # FP: one float4 of four clamped taps per (ray, cell) visit and slice
+TAP_BYTES = 8        # BP: two FP32 taps per pixel-view and slice (a 16-byte pair per 2 slices)
+SINO_BYTES = 4       # FP adjoint: one FP32 sinogram value per (cell, ray) pair and slice
+FMA_FLOP_PER_VISIT = 8  # FP: per visit and slice, two f32x2 FMAs (w . taps)
 
 
 def c1_geometry():
@@ -70,17 +79,43 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profiled_traffic(kernel: str) -> float | None:
-    """DRAM bytes per launch of `kernel` at this workload, from the ncu summary
-    committed under profiles/ (a line 'kernel=<name> dram_bytes_per_launch=<B>')."""
+def profiled(kernel: str, key: str) -> float | None:
+    """A per-launch figure of `kernel` at this workload from the ncu summary
+    committed under profiles/ (lines 'kernel=<name> <key>=<value> ...')."""
     f = REPO / "profiles" / "traffic.txt"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
+        if line.startswith("#"):
+            continue
         parts = dict(kv.split("=", 1) for kv in line.split() if "=" in kv)
-        if parts.get("kernel") == kernel and "dram_bytes_per_launch" in parts:
-            return float(parts["dram_bytes_per_launch"])
+        if parts.get("kernel") == kernel and key in parts:
+            return float(parts[key])
     return None
+
+
+def fp_cell_visits(param16, angles) -> int:
+    """(ray, cell) visits of one FP slice: for each ray, the bilinear cells its
+    samples cross, 1 + |floor(u_last) - floor(u_first)| + |floor(v_last) -
+    floor(v_first)| in cell coordinates (texture coordinates - 1/2), from the
+    library's FP64 ray table.  The kernel gathers one quad per visit."""
+    from fanbeamctrecon_tensorflowop_gb300.geometry import ray_table
+    ray, ns = ray_table(param16, angles)
+    r = ray.reshape(-1, 4).astype(np.float64)
+    n = ns.reshape(-1).astype(np.float64)
+    ok = n > 0
+    u0, v0 = r[ok, 0] - 0.5, r[ok, 1] - 0.5
+    u1 = u0 + (n[ok] - 1.0) * r[ok, 2]
+    v1 = v0 + (n[ok] - 1.0) * r[ok, 3]
+    return int(np.sum(1 + np.abs(np.floor(u1) - np.floor(u0)) + np.abs(np.floor(v1) - np.floor(v0))))
+
+
+def fov_pixels(nx: int, ny: int, xmin: float, ymin: float, dx: float, dy: float, rfov: float) -> int:
+    """Pixels whose centre lies inside the FOV disc (the backprojectors' own
+    double-precision test)."""
+    x = xmin + dx * (np.arange(nx) + 0.5)
+    y = ymin + dy * (np.arange(ny) + 0.5)
+    return int(np.count_nonzero(x[None, :] ** 2 + y[:, None] ** 2 <= float(rfov) * float(rfov)))
 
 
 class ClockSampler:
@@ -148,25 +183,76 @@ def gpu_index_for_smi(local_rank: int) -> int:
     return local_rank
 
 
-def cpu_fp_sample(n_views_sample: int = 24, threads: int | None = None) -> dict:
-    """The oracle's FP (the reference algorithm restated, FP64, OpenMP over all
-    host cores) on a bounded sample: one phantom slice of the clinical
-    geometry, the first n_views_sample views.  Returns G rays/s."""
+# ---- peaks measured in this run (csrc/peaks) -----------------------------------------
+
+def measure_peaks(gpu_index: int) -> dict:
+    """L1 load bandwidth (16-byte read-only loads hitting L1, coalesced) and the
+    FP32 FMA rate (scalar and f32x2), each the best of three launches on the
+    current device, with the SM clock sampled meanwhile."""
+    from fanbeamctrecon_tensorflowop_gb300 import _build
+    _build.build()
+    lib = ctypes.CDLL(str(_build.PEAKS_PATH))
+    d = ctypes.c_double
+    lib.ctpk_l1_load.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(d), ctypes.POINTER(d)]
+    lib.ctpk_fma.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(d),
+                             ctypes.POINTER(d)]
+    lib.ctpk_sm_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    sms = ctypes.c_int()
+    if lib.ctpk_sm_count(ctypes.byref(sms)):
+        raise RuntimeError("ctpk_sm_count failed")
+    out = {"sm_count": sms.value}
+    with ClockSampler(gpu_index) as clk:
+        best = 0.0
+        for _ in range(3):
+            v, ms = d(), d()
+            rc = lib.ctpk_l1_load(4, 2000, ctypes.byref(v), ctypes.byref(ms))
+            if rc:
+                raise RuntimeError(f"ctpk_l1_load failed: CUDA error {rc}")
+            best = max(best, v.value)
+        out["l1_load_gbs"] = best
+        for packed, key in ((0, "fp32_tflops_scalar"), (1, "fp32_tflops_f32x2")):
+            best = 0.0
+            for _ in range(3):
+                v, ms = d(), d()
+                rc = lib.ctpk_fma(packed, 8, 4000, ctypes.byref(v), ctypes.byref(ms))
+                if rc:
+                    raise RuntimeError(f"ctpk_fma failed: CUDA error {rc}")
+                best = max(best, v.value)
+            out[key] = best
+    c = clk.summary()
+    out["fp32_tflops"] = max(out["fp32_tflops_scalar"], out["fp32_tflops_f32x2"])
+    out["clocks"] = c
+    if c.get("sm_mhz"):
+        out["l1_bytes_per_clk_per_sm"] = out["l1_load_gbs"] * 1e9 / (c["sm_mhz"] * 1e6) / sms.value
+    out["how"] = ("csrc/peaks: L1 = 16-byte ld.global.nc over a 32 KiB per-SM buffer, 4 x 512 "
+                  "threads per SM; FP32 = 8 independent FMA chains per thread, scalar and f32x2; "
+                  "best of 3 launches, CUDA events")
+    return out
+
+
+# ---- CPU baseline: FP32 OpenMP transcription of the reference --------------------------
+
+def cpu_baseline(n_views_sample: int = 96) -> dict:
+    """FP, BP and FBP of one clinical slice on the host cores with the FP32
+    transcription, over n_views_sample views spread over the scan."""
     import oracle
+    from oracle import cpu
     from fanbeamctrecon_tensorflowop_gb300 import phantom
     p, a = c1_geometry()
-    ps = p.copy()
-    ps[2] = n_views_sample
-    g = oracle.decode(ps)
+    g = oracle.decode(p)
     img = phantom.ellipse_phantom(N_PIX, PIXEL_MM, seed=0)
-    t0 = time.perf_counter()
-    oracle.fp_fan(g, a[:n_views_sample], img)
-    dt = time.perf_counter() - t0
-    rays = n_views_sample * COLS
-    return {"value": rays / dt / 1e9, "unit": "Grays/s",
-            "cores": threads or os.cpu_count(), "seconds": dt,
-            "sample": f"FP of 1 slice, {n_views_sample} of 984 views x 888 channels "
-                      f"({rays} rays), FP64 oracle, OpenMP"}
+    sino = np.random.default_rng(0).random((VIEWS, COLS)).astype(np.float32)
+    r = cpu.time_ops(g, a, img, sino, n_views_sample)
+    return {
+        "value": r["fp_grays_per_s"], "unit": "Grays/s", "cores": r["threads"], "kind": "port",
+        "cpu": r["cpu"],
+        "sample": (f"one clinical slice, {r['views_timed']} of 984 views (every "
+                   f"{VIEWS // r['views_timed']}th) x 888 channels: FP, BP and Ram-Lak FBP, "
+                   "FP32 OpenMP transcription of the reference (oracle/cpu_fp32.c)"),
+        "bp_gpix_views_per_s": r["bp_gpix_views_per_s"],
+        "fbp_ms_per_slice": r["fbp_ms_per_slice"],
+        "seconds": r["seconds"],
+    }
 
 
 def run_reference(args) -> None:
@@ -174,31 +260,225 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     import oracle
-    oracle.build()
+    from oracle import cpu
+    from fanbeamctrecon_tensorflowop_gb300 import phantom
+    cpu.build()
+    p, a = c1_geometry()
+    g = oracle.decode(p)
+    img = phantom.ellipse_phantom(N_PIX, PIXEL_MM, seed=0)
+    nv = 123  # views per step: one eighth of the scan, every 8th view
+    sel = np.arange(0, VIEWS, VIEWS // nv)[:nv]
+    sub = oracle.OrcGeom.from_buffer_copy(g)
+    sub.n_views = nv
+    sa = np.ascontiguousarray(a[sel])
     for _ in range(args.warmup):
-        cpu_fp_sample(8)
-    vals, secs = [], 0.0
-    res = None
+        cpu.fp_fan(sub, sa, img)
+    secs = []
     for _ in range(args.steps):
-        res = cpu_fp_sample(24)
-        vals.append(res["value"])
-        secs += res["seconds"]
-    v = statistics.median(vals)
+        t0 = time.perf_counter()
+        cpu.fp_fan(sub, sa, img)
+        secs.append(time.perf_counter() - t0)
+    total = sum(secs)
+    v = args.steps * nv * COLS / total / 1e9
+    others = cpu_baseline(96)
+    sample = (f"FP of one clinical slice per step, {nv} of 984 views (every 8th) x 888 "
+              f"channels ({nv * COLS} rays), FP32 OpenMP transcription of the reference "
+              "(oracle/cpu_fp32.c)")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Grays/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * secs / max(1, args.steps), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "ms_per_step": 1e3 * total / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded ellipse phantom (numpy default_rng seed 0)",
-        "config": {"workload": WORKLOAD, "sample": res["sample"],
+        "config": {"workload": WORKLOAD, "sample": sample,
                    "note": "the reference's CUDA/TF ops cannot be built for the GPU (CUDA 13 "
-                           "rejects texture references; TF/IPP absent): its algorithm runs "
-                           "as the FP64 oracle restatement on the host cores"},
-        "cpu_baseline": {"value": v, "unit": "Grays/s", "cores": res["cores"], "kind": "port",
-                         "sample": res["sample"]},
+                           "rejects texture references; TF/IPP absent): its algorithms run "
+                           "as an FP32 OpenMP transcription on the host cores"},
+        "cpu_baseline": {"value": v, "unit": "Grays/s", "cores": cpu.threads(), "kind": "port",
+                         "cpu": cpu.cpu_model(), "sample": sample,
+                         "bp_gpix_views_per_s": others["bp_gpix_views_per_s"],
+                         "fbp_ms_per_slice": others["fbp_ms_per_slice"]},
         "e2e": {"value": v, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+# ---- output errors against the FP64 oracle (the checker), untimed ----------------------
+
+def _rel(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def oracle_errors(dev, plan, plan_sl, imgs, usinos) -> dict:
+    """Relative L2 of each output against the FP64 oracle on the same inputs,
+    and the adjoints' dot-product mismatches, at each workload's own image
+    and detector size (views subsampled where the oracle's cost needs it)."""
+    import torch
+
+    import oracle
+    from fanbeamctrecon_tensorflowop_gb300 import _lib
+    from fanbeamctrecon_tensorflowop_gb300.batch import UnevenBatch
+    from fanbeamctrecon_tensorflowop_gb300.geometry import angle, fan_param16
+    from fanbeamctrecon_tensorflowop_gb300.ops import ConePlan, FanPlan
+
+    t_start = time.perf_counter()
+    out: dict = {"tolerance": 1e-4, "against": "FP64 oracle (oracle/oracle.c)"}
+    p, a = c1_geometry()
+    g = oracle.decode(p)
+    every = 4
+    sel = np.arange(0, VIEWS, every)
+    sub = oracle.OrcGeom.from_buffer_copy(g)
+    sub.n_views = len(sel)
+    asub = np.ascontiguousarray(a[sel])
+
+    x = imgs[0][:1]
+    sino = plan.fp(x)
+    c1 = {}
+    c1["fp"] = _rel(sino[0].cpu().numpy()[sel], oracle.fp_fan(sub, asub, x[0].cpu().numpy())[0])
+    u = usinos[0][:1]
+    c1["bp"] = _rel(plan.bp(u)[0].cpu().numpy(), oracle.bp_fan(g, a, u[0].cpu().numpy())[0])
+    c1["fbp_shepp_logan"] = _rel(plan_sl.fbp(sino)[0].cpu().numpy(),
+                                 oracle.fbp_fan(g, a, sino[0].cpu().numpy(),
+                                                window=oracle.SHEPP_LOGAN)[0])
+    gen = torch.Generator(device=dev).manual_seed(7)
+    y = torch.randn((1, VIEWS, COLS), device=dev, generator=gen)
+    ymask = torch.zeros_like(y)
+    ymask[:, sel] = y[:, sel]
+    c1["fp_adjoint"] = _rel(plan.fp_adjoint(ymask)[0].cpu().numpy(),
+                            oracle.fp_fan_adjoint(sub, asub, y[0].cpu().numpy()[sel])[0])
+    c1["fbp_adjoint"] = _rel(plan_sl.fbp_adjoint(x)[0].cpu().numpy(),
+                             oracle.fbp_fan_adjoint(g, a, x[0].cpu().numpy(),
+                                                    window=oracle.SHEPP_LOGAN)[0])
+    c1["views_compared"] = {"fp": f"every {every}th view", "fp_adjoint": f"sinogram nonzero on "
+                            f"every {every}th view", "bp": "all", "fbp": "all"}
+    out["clinical_512_984x888"] = c1
+
+    # dot-product mismatches |<Ax, y> - <x, A^T y>| / |<Ax, y>| at batch 32
+    xs = torch.randn((BATCH, N_PIX, N_PIX), device=dev, generator=gen)
+    ys = torch.randn((BATCH, VIEWS, COLS), device=dev, generator=gen)
+
+    def dot(u_, v_):
+        return float((u_.double() * v_.double()).sum())
+
+    l_, r_ = dot(plan.fp(xs), ys), dot(xs, plan.fp_adjoint(ys))
+    dots = {"fp_batch32": abs(l_ - r_) / abs(l_)}
+    l_, r_ = dot(plan_sl.fbp(ys), xs), dot(ys, plan_sl.fbp_adjoint(xs))
+    dots["fbp_batch32"] = abs(l_ - r_) / abs(l_)
+    l_, r_ = dot(plan.bp(ys), xs), dot(ys, plan.bp_adjoint(xs))
+    dots["bp_batch32"] = abs(l_ - r_) / abs(l_)
+    del xs, ys
+
+    # uneven BF16 batch: one slice of each of the three geometries, FP / FBP / FBP adjoint
+    unev = {}
+    for n_, v_, c_ in ((256, 492, 512), (384, 720, 736), (512, 984, 888)):
+        up = fan_param16(sdd=SDD, sid=SID, n_views=v_, n_cols=c_, n=n_, pixel_mm=358.4 / n_,
+                         dcol_rad=DCOL)
+        ua = angle(v_, 0.0)
+        pl = FanPlan(up, ua, device=dev)
+        ug = oracle.decode(up)
+        img16 = torch.rand((n_, n_), device=dev, generator=gen).to(torch.bfloat16)
+        sino16 = torch.rand(pl.sino_shape, device=dev, generator=gen).to(torch.bfloat16)
+        o_fp = torch.empty(pl.sino_shape, device=dev, dtype=torch.bfloat16)
+        o_fbp = torch.empty(pl.image_shape, device=dev, dtype=torch.bfloat16)
+        o_adj = torch.empty(pl.sino_shape, device=dev, dtype=torch.bfloat16)
+        for it in ((pl, "fp", img16, o_fp), (pl, "fbp", sino16, o_fbp),
+                   (pl, "fbp_adjoint", img16, o_adj)):
+            UnevenBatch([it]).run()
+        xi = img16.float().cpu().numpy()
+        si = sino16.float().cpu().numpy()
+        unev[f"{n_}^2_{v_}x{c_}"] = {
+            "fp": _rel(o_fp.float().cpu().numpy(), oracle.fp_fan(ug, ua, xi)[0]),
+            "fbp": _rel(o_fbp.float().cpu().numpy(), oracle.fbp_fan(ug, ua, si)[0]),
+            "fbp_adjoint": _rel(o_adj.float().cpu().numpy(),
+                                oracle.fbp_fan_adjoint(ug, ua, xi)[0]),
+        }
+        pl.close()
+    unev["note"] = ("BF16 storage: the oracle runs on the BF16-rounded inputs, the outputs "
+                    "are rounded to BF16 (2^-9 relative per value)")
+    out["uneven_bf16"] = unev
+
+    # cone beam at the clinical volume and detector (512^2 x 64, 888 x 64), 8 views
+    nvc = 8
+    csel = np.arange(0, VIEWS, VIEWS // nvc)[:nvc]
+    cp = fan_param16(sdd=SDD, sid=SID, n_views=nvc, n_cols=COLS, n=N_PIX, pixel_mm=PIXEL_MM,
+                     dcol_rad=DCOL, det_bottom=-32.0, drow=1.0, dz=0.625)
+    ca = np.ascontiguousarray(a[csel])
+    cplan = ConePlan(cp, ca, 64, 64, device=dev)
+    cg = oracle.decode(cp)
+    vol = torch.rand((1, 64, N_PIX, N_PIX), device=dev, generator=gen)
+    proj = cplan.fp_cone(vol)
+    rec = cplan.fdk(proj)
+    cadj = cplan.fdk_adjoint(vol)
+    vn, pn = vol[0].cpu().numpy(), proj[0].cpu().numpy()
+    out["cone_512x512x64_888x64"] = {
+        "fp_cone": _rel(pn, oracle.cone_fp(cg, 64, 64, ca, vn)[0]),
+        "fdk": _rel(rec[0].cpu().numpy(), oracle.fdk_cone(cg, 64, 64, ca, pn)[0]),
+        "fdk_adjoint": _rel(cadj[0].cpu().numpy(), oracle.fdk_cone_adjoint(cg, 64, 64, ca, vn)[0]),
+        "views": f"{nvc} of 984 (every {VIEWS // nvc}th)",
+    }
+    yc = torch.randn((1, nvc, 64, COLS), device=dev, generator=gen)
+    l_, r_ = dot(cplan.fdk(yc), vol), dot(yc, cplan.fdk_adjoint(vol))
+    dots["fdk_cone"] = abs(l_ - r_) / abs(l_)
+    cplan.close()
+    out["dot_mismatch"] = dots
+    f32 = [v for d in (c1, out["cone_512x512x64_888x64"]) for v in d.values()
+           if isinstance(v, float)]
+    bf16 = [v for d in unev.values() if isinstance(d, dict) for v in d.values()]
+    out["worst_rel_l2_f32"] = max(f32)
+    out["worst_rel_l2_bf16"] = max(bf16)
+    out["worst_dot_mismatch"] = max(dots.values())
+    out["seconds"] = time.perf_counter() - t_start
+    return out
+
+
+# ---- profiler driver -------------------------------------------------------------------
+
+def profile_case(args) -> None:
+    """Runs one operator on the clinical-scale geometry: one untimed warm-up
+    call, then ``--iters`` calls, so ``ncu -s <launches of one call>`` skips the
+    warm-up.  Ops: fp, fp_adjoint, bp, bp_adjoint, filter, fbp, fbp_adjoint
+    (``--batch`` slices); cone_fp, fdk, fdk_adjoint (``--batch`` volumes of
+    512^2 x 64 voxels at 0.7 x 0.7 x 0.625 mm, 888 x 64 detector cells of 1 mm
+    rows per view)."""
+    import torch
+
+    from fanbeamctrecon_tensorflowop_gb300 import _lib, phantom
+    from fanbeamctrecon_tensorflowop_gb300.geometry import angle, fan_param16
+    from fanbeamctrecon_tensorflowop_gb300.ops import ConePlan, FanPlan
+
+    dev = torch.device("cuda", 0)
+    op = args.profile_case
+    n, views, cols, pixel = args.n, args.views, COLS, PIXEL_MM
+    a = angle(views, 0.0)
+    if op in ("cone_fp", "fdk", "fdk_adjoint"):
+        pc = fan_param16(sdd=SDD, sid=SID, n_views=views, n_cols=cols, n=n, pixel_mm=pixel,
+                         dcol_rad=DCOL, det_bottom=-32.0, drow=1.0, dz=0.625)
+        cplan = ConePlan(pc, a, 64, 64, device=dev)
+        vol = torch.rand((args.batch, 64, n, n), device=dev)
+        proj = cplan.fp_cone(vol)
+        fn = {"cone_fp": lambda: cplan.fp_cone(vol, out=proj),
+              "fdk": lambda: cplan.fdk(proj),
+              "fdk_adjoint": lambda: cplan.fdk_adjoint(vol)}[op]
+    else:
+        p = fan_param16(sdd=SDD, sid=SID, n_views=views, n_cols=cols, n=n, pixel_mm=pixel,
+                        dcol_rad=DCOL)
+        win = _lib.WINDOW_SHEPP_LOGAN if args.window == "shepp_logan" else _lib.WINDOW_RAMLAK
+        plan = FanPlan(p, a, device=dev, window=win)
+        img = torch.from_numpy(np.stack([phantom.ellipse_phantom(n, pixel, seed=s)
+                                         for s in range(args.batch)])).to(dev)
+        sino = plan.fp(img)
+        fn = {"fp": lambda: plan.fp(img), "fp_adjoint": lambda: plan.fp_adjoint(sino),
+              "bp": lambda: plan.bp(sino), "bp_adjoint": lambda: plan.bp_adjoint(img),
+              "filter": lambda: plan.ramp_filter(sino), "fbp": lambda: plan.fbp(sino),
+              "fbp_adjoint": lambda: plan.fbp_adjoint(img)}[op]
+    fn()
+    torch.cuda.synchronize()
+    for _ in range(args.iters):
+        fn()
+    torch.cuda.synchronize()
+    print(f"profile_case {op} batch={args.batch} ok")
 
 
 def main() -> None:
@@ -207,11 +487,22 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU baseline and the oracle error checks")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cone", action="store_true")
     ap.add_argument("--no-uneven", action="store_true")
+    ap.add_argument("--profile-case", default=None,
+                    help="run one operator for a profiler instead of the benchmark")
+    ap.add_argument("--batch", type=int, default=8, help="--profile-case: slices or volumes")
+    ap.add_argument("--iters", type=int, default=3, help="--profile-case: profiled calls")
+    ap.add_argument("--views", type=int, default=VIEWS, help="--profile-case: views")
+    ap.add_argument("--n", type=int, default=N_PIX, help="--profile-case: image size")
+    ap.add_argument("--window", default="ramlak", choices=["ramlak", "shepp_logan"])
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         run_reference(args)
@@ -231,6 +522,7 @@ def main() -> None:
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    smi = gpu_index_for_smi(local)
 
     p, a = c1_geometry()
     plan = FanPlan(p, a, device=dev)
@@ -286,45 +578,71 @@ def main() -> None:
         per = [e0.elapsed_time(e1) / 1e3 for e0, e1 in evs]
         return max_over_ranks(total), per, n1 - n0
 
+    # ---- peaks of this GPU, measured now (untimed) ----------------------------------
+    pk = measure_peaks(smi)
+    hbm = measured_peaks()
+
     # ---- headline: FP throughput -----------------------------------------------
     def fp_step(k):
         plan.fp(imgs[k % POOL], out=sinos[k % POOL])
 
-    with ClockSampler(gpu_index_for_smi(local)) as clk:
+    with ClockSampler(smi) as clk:
         total_fp, per_fp, launches = timed(fp_step, args.steps, args.warmup)
     rays_per_step = BATCH * VIEWS * COLS
     value = world * rays_per_step * args.steps / total_fp / 1e9
     ms_per_step = 1e3 * total_fp / args.steps
 
-    # roofline of the dominant (only) kernel of the step: fp_fan_kernel
-    peaks = measured_peaks()
-    samples_per_launch = BATCH * plan.total_samples
-    mean_launch = sum(per_fp) / len(per_fp)
-    achieved_gbs = GATHER_BYTES_PER_SAMPLE * samples_per_launch / mean_launch / 1e9
-    traffic = profiled_traffic("fp_fan_kernel")
-    fp32_tflops = FLOP_PER_SAMPLE * samples_per_launch / mean_launch / 1e12
-    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
-                "traffic": traffic, "peak_source": peaks["source"],
-                "kernel": "fp_fan_kernel",
-                "algorithmic": f"{GATHER_BYTES_PER_SAMPLE} B/sample x {samples_per_launch:.4g} "
-                               "samples per launch (effective bilinear gather bytes)",
-                "timed": "per-step CUDA events (the step is build_quads_kernel + "
-                         "fp_fan_kernel; the quad build is ~3% of it)",
-                "note": "the cell walk sums each cell's ~6 samples in closed form, so per-sample "
-                        "work runs above the per-sample peaks; DRAM is far from the bound",
-                "dram_gbs": (traffic / mean_launch / 1e9) if traffic else None,
-                "fp32": {"achieved_tflops": fp32_tflops, "peak_tflops": FP32_PEAK_TFLOPS,
-                         "frac": fp32_tflops / FP32_PEAK_TFLOPS,
-                         "peak_source": "derived: 152 SMs x 128 x 2 FLOP x 2.07 GHz",
-                         "algorithmic": f"{FLOP_PER_SAMPLE} FLOP/sample"}}
+    # roofline of the dominant kernel of the step, fp_fan_kernel (98% of the step:
+    # build_quads_kernel + fp_fan_kernel; profiles/bench_launches_c1.md)
+    visits = fp_cell_visits(p, a)
+    mean_fp = sum(per_fp) / len(per_fp)
+    share = profiled("fp_fan_kernel", "share_of_step") or 1.0
+    kern_s = mean_fp * share
+    l1_bytes = QUAD_BYTES * BATCH * visits
+    achieved = l1_bytes / kern_s / 1e9
+    traffic = profiled("fp_fan_kernel", "dram_bytes_per_launch")
+    compulsory = 4.0 * (N_PIX * N_PIX + VIEWS * COLS) * BATCH
+    roofline = {
+        "bound": "l1", "achieved": achieved, "peak": pk["l1_load_gbs"], "unit": "GB/s",
+        "frac": achieved / pk["l1_load_gbs"], "traffic": traffic,
+        "peak_source": "measured in this run (csrc/peaks: coalesced 16-byte L1-hit loads)",
+        "kernel": "fp_fan_kernel",
+        "algorithmic": (f"{QUAD_BYTES} B (one float4 quad) per (ray, cell) visit and slice x "
+                        f"{visits} visits per slice x {BATCH} slices = {l1_bytes:.4g} B per launch"),
+        "timed": (f"per-step CUDA events x the kernel's share of the step ({share:.3f}, "
+                  "profiles/traffic.txt)"),
+        "kernel_ms": 1e3 * kern_s,
+        "dram": {"compulsory_bytes": compulsory,
+                 "compulsory_frac_of_hbm": compulsory / kern_s / 1e9 / hbm["hbm_gbs"],
+                 "measured_bytes": traffic,
+                 "measured_frac_of_hbm": (traffic / kern_s / 1e9 / hbm["hbm_gbs"]) if traffic
+                 else None,
+                 "hbm_peak_gbs": hbm["hbm_gbs"], "hbm_peak_source": hbm["source"]},
+        "fp32": {"achieved_tflops": FMA_FLOP_PER_VISIT * BATCH * visits / kern_s / 1e12,
+                 "peak_tflops": pk["fp32_tflops"],
+                 "frac": FMA_FLOP_PER_VISIT * BATCH * visits / kern_s / 1e12 / pk["fp32_tflops"],
+                 "algorithmic": f"{FMA_FLOP_PER_VISIT} FLOP (two f32x2 FMAs) per visit and slice",
+                 "peak_source": "measured in this run (csrc/peaks FMA chains)"},
+    }
 
     # ---- BP throughput ------------------------------------------------------------
     def bp_step(k):
         plan.bp(usinos[k % POOL], out=bimgs[k % POOL])
 
-    total_bp, _, _ = timed(bp_step, args.steps, args.warmup)
+    total_bp, per_bp, _ = timed(bp_step, args.steps, args.warmup)
     bp_gpv = world * BATCH * N_PIX * N_PIX * VIEWS * args.steps / total_bp / 1e9
+    fovpix = fov_pixels(g.nx, g.ny, g.xmin, g.ymin, g.dx, g.dy, g.rfov)
+    bp_share = profiled("bp_fan_kernel", "share_of_step") or 1.0
+    bp_s = sum(per_bp) / len(per_bp) * bp_share
+    bp_bytes = TAP_BYTES * BATCH * fovpix * VIEWS
+    bp_roof = {"bound": "l1", "kernel": "bp_fan_kernel", "achieved": bp_bytes / bp_s / 1e9,
+               "peak": pk["l1_load_gbs"], "unit": "GB/s",
+               "frac": bp_bytes / bp_s / 1e9 / pk["l1_load_gbs"],
+               "algorithmic": (f"{TAP_BYTES} B (two FP32 taps) per in-FOV pixel-view and slice "
+                               f"x {fovpix} pixels x {VIEWS} views x {BATCH} slices"),
+               "share_of_step": bp_share,
+               "dram_compulsory_frac_of_hbm": 4.0 * (N_PIX * N_PIX + VIEWS * COLS) * BATCH
+               / bp_s / 1e9 / hbm["hbm_gbs"]}
 
     # ---- Shepp-Logan FBP of the FP sinograms ----------------------------------------
     def fbp_step(k):
@@ -351,8 +669,28 @@ def main() -> None:
 
     total_adj, per_adj, _ = timed(adj_step, n_fa, args.warmup)
     adj_ms = 1e3 * total_adj / n_fa
-    adj_gather_gbs = GATHER_BYTES_PER_SAMPLE * samples_per_launch / (
-        sum(per_adj) / len(per_adj)) / 1e9
+    adj_share = profiled("fp_adjoint_cells_kernel", "share_of_step") or 1.0
+    adj_s = sum(per_adj) / len(per_adj) * adj_share
+    adj_bytes = SINO_BYTES * BATCH * visits
+    adj_roof = {"bound": "issue", "kernel": "fp_adjoint_cells_kernel",
+                "achieved": adj_bytes / adj_s / 1e9, "peak": pk["l1_load_gbs"], "unit": "GB/s",
+                "frac": adj_bytes / adj_s / 1e9 / pk["l1_load_gbs"],
+                "algorithmic": (f"{SINO_BYTES} B (one FP32 sinogram value) per (cell, ray) pair "
+                                f"and slice x {visits} pairs per slice x {BATCH} slices"),
+                "share_of_step": adj_share}
+
+    # ---- BP / FBP adjoints (transposes) -------------------------------------------
+    def bpt_step(k):
+        plan.bp_adjoint(imgs[k % POOL], out=sinos[k % POOL])
+
+    total_bpt, _, _ = timed(bpt_step, n_fa, args.warmup)
+    bpt_ms = 1e3 * total_bpt / n_fa
+
+    def fbpt_step(k):
+        plan_sl.fbp_adjoint(imgs[k % POOL], out=sinos[k % POOL])
+
+    total_fbpt, _, _ = timed(fbpt_step, n_fa, args.warmup)
+    fbpt_ms = 1e3 * total_fbpt / n_fa
 
     plain_ms = None
     if not args.no_plain:
@@ -405,6 +743,7 @@ def main() -> None:
                 "fdk_adjoint_ms_per_volume": t_adj,
                 "fdk_gvoxel_views_per_s": 512 * 512 * 64 * VIEWS / t_fdk / 1e6}
         del cvol, cproj, crec, cgrad
+        cplan.close()
 
     # ---- uneven batches, BF16 storage; FP, FBP and FBP adjoint of all 48 slices as
     #      three ct_batch_run calls recorded in one CUDA graph:
@@ -514,10 +853,11 @@ def main() -> None:
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_val = world * rays_per_step * n_e2e / e2e_s / 1e9
 
-    cpu = None
+    cpu = errors = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_fp_sample(24)
+        cpu = cpu_baseline(96)
         cpu.pop("seconds", None)
+        errors = oracle_errors(dev, plan, plan_sl, imgs, usinos)
 
     if rank == 0:
         line = {
@@ -536,15 +876,21 @@ def main() -> None:
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
+            "peaks": pk,
+            "errors": errors,
             "secondary": {
                 "bp_gpix_views_per_s": bp_gpv,
+                "bp_roofline": bp_roof,
                 "fbp_shepp_logan_ms_per_slice": fbp_ms_per_slice,
                 "batch32_fp_adjoint_ms": fa_ms,
                 "batch32_adjoint_only_ms": adj_ms,
-                "adjoint_effective_gather_gbs": adj_gather_gbs,
+                "fp_adjoint_roofline": adj_roof,
+                "batch32_bp_adjoint_ms": bpt_ms,
+                "batch32_fbp_adjoint_ms": fbpt_ms,
                 "plain_batch32_fp_adjoint_ms": plain_ms,
                 "speedup_vs_plain": (plain_ms / fa_ms) if plain_ms else None,
                 "fp_samples_per_slice": plan.total_samples,
+                "fp_cell_visits_per_slice": visits,
                 "cone": cone,
                 "uneven_bf16": uneven,
                 "uneven_distinct_bf16": uneven_distinct,

@@ -2,7 +2,9 @@
 
 Every translation unit compiles in parallel with nvcc/g++; the shared library
 links the CUDA runtime statically so it depends only on the driver.  Objects
-and the library go to ``_build/`` next to this file.
+and the library go to ``_build/`` next to this file.  The same pass builds
+libctpeaks.so (``csrc/peaks``): the L1-load and FP32 microbenchmarks that give
+the benchmark its roofline denominators; no operator uses it.
 """
 from __future__ import annotations
 
@@ -21,6 +23,8 @@ INCLUDE = REPO_DIR / "include"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_NAME = "libctgb.so"
 LIB_PATH = BUILD_DIR / LIB_NAME
+PEAKS_SRC = CSRC / "peaks" / "peaks.cu"
+PEAKS_PATH = BUILD_DIR / "libctpeaks.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -55,6 +59,7 @@ def _fingerprint() -> str:
     for p in _sources() + _headers():
         h.update(p.name.encode())
         h.update(p.read_bytes())
+    h.update(PEAKS_SRC.read_bytes())
     h.update(" ".join(NVCC_FLAGS + CXX_FLAGS).encode())
     h.update(os.uname().machine.encode())
     return h.hexdigest()
@@ -80,17 +85,26 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     stamp = BUILD_DIR / "stamp.txt"
     fp = _fingerprint()
-    if not force and LIB_PATH.exists() and stamp.exists() and stamp.read_text() == fp:
+    if (not force and LIB_PATH.exists() and PEAKS_PATH.exists() and stamp.exists()
+            and stamp.read_text() == fp):
         return LIB_PATH
     srcs = _sources()
-    with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, min(len(srcs) + 1, os.cpu_count() or 4))) as ex:
+        peaks = ex.submit(_compile, PEAKS_SRC)
         objs = list(ex.map(_compile, srcs))
+        peaks_obj = peaks.result()
     tmp = BUILD_DIR / (LIB_NAME + ".tmp")
     cmd = [_nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB_PATH)
+    tmp = BUILD_DIR / "libctpeaks.so.tmp"
+    cmd = [_nvcc(), "-shared", *ARCH, "-o", str(tmp), str(peaks_obj)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, PEAKS_PATH)
     stamp.write_text(fp)
     if verbose:
         print(f"built {LIB_PATH}")

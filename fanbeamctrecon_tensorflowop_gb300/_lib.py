@@ -80,6 +80,17 @@ class CtBatchConfig(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+# ct_allocator: alloc(ctx, bytes, stream) -> ptr, free(ctx, ptr, stream)
+ALLOC_FN = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p)
+FREE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)
+
+
+class CtAllocator(ctypes.Structure):
+    """Mirror of ct_allocator."""
+
+    _fields_ = [("ctx", ctypes.c_void_p), ("alloc", ALLOC_FN), ("free", FREE_FN)]
+
+
 class CtPlanOpts(ctypes.Structure):
     _fields_ = [("filter_window", ctypes.c_int32), ("filter_algo", ctypes.c_int32),
                 ("short_scan", ctypes.c_int32), ("cosine_weight", ctypes.c_int32),
@@ -97,6 +108,8 @@ SIGNATURES = {
     "ct_version": (ctypes.c_char_p, []),
     "ct_last_error": (ctypes.c_char_p, []),
     "ct_launch_count": (ctypes.c_uint64, []),
+    "ct_set_allocator": (_i, [_P(CtAllocator)]),
+    "ct_device_alloc_count": (ctypes.c_uint64, []),
     "ct_geom_from_param16": (_i, [_P(ctypes.c_float), _P(CtFanGeom)]),
     "ct_fp_ray_table": (_i, [_P(CtFanGeom), _P(ctypes.c_float), _i, _P(ctypes.c_float),
                             _P(ctypes.c_int32)]),

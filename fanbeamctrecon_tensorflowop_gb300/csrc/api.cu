@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -13,6 +14,47 @@ namespace {
 
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
+
+// Device memory: the caller's allocator (ct_set_allocator) or, when none is
+// set, the CUDA runtime.  Every allocation the library makes goes through
+// dev_alloc, which counts the successful ones (ct_device_alloc_count).
+std::mutex g_alloc_mu;
+ct_allocator g_alloc{};  // alloc == NULL: cudaMalloc / cudaMallocAsync
+std::atomic<uint64_t> g_alloc_count{0};
+
+ct_allocator current_allocator() {
+    std::lock_guard<std::mutex> lock(g_alloc_mu);
+    return g_alloc;
+}
+
+// stream_ordered: scratch of one call (cudaMallocAsync on `s`); otherwise a
+// plan table (cudaMalloc).
+cudaError_t dev_alloc(const ct_allocator &a, void **p, size_t bytes, cudaStream_t s,
+                      bool stream_ordered) {
+    *p = nullptr;
+    if (a.alloc) {
+        *p = a.alloc(a.ctx, bytes, reinterpret_cast<ct_stream>(s));
+        if (!*p) return cudaErrorMemoryAllocation;
+    } else {
+        cudaError_t e = stream_ordered ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            *p = nullptr;
+            return e;
+        }
+    }
+    g_alloc_count.fetch_add(1, std::memory_order_relaxed);
+    return cudaSuccess;
+}
+
+void dev_free(const ct_allocator &a, void *p, cudaStream_t s, bool stream_ordered) {
+    if (!p) return;
+    if (a.alloc)
+        a.free(a.ctx, p, reinterpret_cast<ct_stream>(s));
+    else if (stream_ordered)
+        cudaFreeAsync(p, s);
+    else
+        cudaFree(p);
+}
 
 ct_status cuda_status(cudaError_t e, const char *where) {
     if (e == cudaSuccess) return CT_OK;
@@ -45,8 +87,9 @@ struct Workspace {
     void *ptr = nullptr;
     bool owned = false;
     cudaStream_t stream = nullptr;
+    ct_allocator alloc{};
     ~Workspace() {
-        if (owned && ptr) cudaFreeAsync(ptr, stream);
+        if (owned && ptr) dev_free(alloc, ptr, stream, true);
     }
 };
 
@@ -65,8 +108,9 @@ ct_status acquire(Workspace &w, void *given, size_t given_bytes, size_t need, cu
         w.ptr = given;
         return CT_OK;
     }
-    cudaError_t e = cudaMallocAsync(&w.ptr, need, s);
-    if (e != cudaSuccess) return cuda_status(e, "cudaMallocAsync(workspace)");
+    w.alloc = current_allocator();
+    cudaError_t e = dev_alloc(w.alloc, &w.ptr, need, s, true);
+    if (e != cudaSuccess) return cuda_status(e, "device allocation (workspace)");
     w.owned = true;
     return CT_OK;
 }
@@ -133,27 +177,23 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
 
 void free_plan(ct_plan *p) {
     if (!p) return;
-    cudaFree(p->d_view_cs);
-    cudaFree(p->d_ray);
-    cudaFree(p->d_ray_inv);
-    cudaFree(p->d_nsamp);
-    cudaFree(p->d_taps);
-    cudaFree(p->d_chan_s);
-    cudaFree(p->d_tc_hi);
-    cudaFree(p->d_tc_lo);
-    cudaFree(p->d_err);
-    cudaFree(p->d_parker);
-    cudaFree(p->d_cosw);
-    cudaFree(p->d_view_z);
+    for (void *t : {(void *)p->d_view_cs, (void *)p->d_ray, (void *)p->d_ray_inv,
+                    (void *)p->d_nsamp, (void *)p->d_taps, (void *)p->d_chan_s,
+                    (void *)p->d_tc_hi, (void *)p->d_tc_lo, (void *)p->d_err,
+                    (void *)p->d_parker, (void *)p->d_cosw, (void *)p->d_view_z})
+        dev_free(p->alloc, t, nullptr, false);
     delete p;
 }
 
+// Allocates a plan table with the plan's allocator and copies `src` into it.
 template <typename T>
-ct_status upload(T **dst, const std::vector<T> &src) {
+ct_status upload(const ct_plan *p, T **dst, const std::vector<T> &src) {
     *dst = nullptr;
     if (src.empty()) return CT_OK;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dst), sizeof(T) * src.size());
-    if (e != cudaSuccess) return cuda_status(e, "cudaMalloc(plan table)");
+    void *d = nullptr;
+    cudaError_t e = dev_alloc(p->alloc, &d, sizeof(T) * src.size(), nullptr, false);
+    if (e != cudaSuccess) return cuda_status(e, "device allocation (plan table)");
+    *dst = static_cast<T *>(d);
     e = cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice);
     return cuda_status(e, "cudaMemcpy(plan table)");
 }
@@ -207,6 +247,19 @@ const char *ct_version(void) { return "ctgb 0.1.0 (sm_103a)"; }
 const char *ct_last_error(void) { return g_last_error.c_str(); }
 
 uint64_t ct_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+ct_status ct_set_allocator(const ct_allocator *allocator) {
+    ct_allocator a{};
+    if (allocator) {
+        if (!allocator->alloc || !allocator->free) return CT_ERR_NULL_POINTER;
+        a = *allocator;
+    }
+    std::lock_guard<std::mutex> lock(g_alloc_mu);
+    g_alloc = a;
+    return CT_OK;
+}
+
+uint64_t ct_device_alloc_count(void) { return g_alloc_count.load(std::memory_order_relaxed); }
 
 ct_status ct_geom_from_param16(const float param[16], ct_fan_geom *out) {
     return ct_decode_param16(param, out);
@@ -304,33 +357,36 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
     p->total_samples = t.total_samples;
     p->max_nsamp = t.max_nsamp;
     p->h_view_cs = t.view_cs;
+    p->alloc = current_allocator();
     cudaError_t e = cudaGetDevice(&p->device);
     if (e != cudaSuccess) {
         delete p;
         return cuda_status(e, "cudaGetDevice");
     }
-    if ((st = upload(&p->d_view_cs, t.view_cs)) != CT_OK ||
-        (st = upload(&p->d_ray, t.ray)) != CT_OK || (st = upload(&p->d_nsamp, t.nsamp)) != CT_OK ||
-        (st = upload(&p->d_ray_inv, ray_inv)) != CT_OK ||
-        (st = upload(&p->d_taps, t.taps)) != CT_OK ||
-        (st = upload(&p->d_chan_s, t.chan_s)) != CT_OK ||
-        (st = upload(&p->d_parker, t.parker)) != CT_OK ||
-        (st = upload(&p->d_cosw, t.cosw)) != CT_OK ||
-        (st = upload(&p->d_view_z, t.view_z)) != CT_OK) {
+    if ((st = upload(p, &p->d_view_cs, t.view_cs)) != CT_OK ||
+        (st = upload(p, &p->d_ray, t.ray)) != CT_OK ||
+        (st = upload(p, &p->d_nsamp, t.nsamp)) != CT_OK ||
+        (st = upload(p, &p->d_ray_inv, ray_inv)) != CT_OK ||
+        (st = upload(p, &p->d_taps, t.taps)) != CT_OK ||
+        (st = upload(p, &p->d_chan_s, t.chan_s)) != CT_OK ||
+        (st = upload(p, &p->d_parker, t.parker)) != CT_OK ||
+        (st = upload(p, &p->d_cosw, t.cosw)) != CT_OK ||
+        (st = upload(p, &p->d_view_z, t.view_z)) != CT_OK) {
         free_plan(p);
         return st;
     }
     if (p->filter_algo == CT_FILTER_TOEPLITZ_TC) {
         std::vector<float> hi, lo;
         ctk::build_tc_taps(t.taps.data(), geom->n_cols, hi, lo);
-        if ((st = upload(&p->d_tc_hi, hi)) != CT_OK || (st = upload(&p->d_tc_lo, lo)) != CT_OK) {
+        if ((st = upload(p, &p->d_tc_hi, hi)) != CT_OK ||
+            (st = upload(p, &p->d_tc_lo, lo)) != CT_OK) {
             free_plan(p);
             return st;
         }
     }
     {
         const std::vector<int> zero(1, 0);
-        if ((st = upload(&p->d_err, zero)) != CT_OK) {
+        if ((st = upload(p, &p->d_err, zero)) != CT_OK) {
             free_plan(p);
             return st;
         }

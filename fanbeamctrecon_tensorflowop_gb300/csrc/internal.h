@@ -54,6 +54,7 @@ int ct_fit_atan(double zmax, float coef[9]);
 struct ct_plan {
     ct_fan_geom g;
     ct_plan_opts opts;
+    ct_allocator alloc;              // allocator of the tables below (ct_set_allocator)
     int device;
     int filter_algo;                 // resolved ct_filter_algo (never AUTO)
     float fp_weight;                 // 0.125*dx (FP/transform.cu:144)

@@ -9,10 +9,15 @@
 // serves them from a fixed array in this library's own device memory.
 //
 // The array is a file-scope __device__ variable: every GPU on which this
-// library's device code is loaded holds its CT_FBP_STATIC_SCRATCH_FLOATS
-// floats until the process exits.  Host code cannot use the symbol itself as a
-// device address, so the first call on each device looks up the array's
-// device address once, with that device current, and caches it.
+// file's device code is loaded holds its CT_FBP_STATIC_SCRATCH_FLOATS floats
+// until the process exits.  The CUDA runtime loads a module lazily (by
+// default since CUDA 12.2), so the array is reserved when the first call on a
+// device looks up its address: that first call, the set-up, takes the 32 MiB
+// and can fail with CT_ERR_ALLOC when the device is full.  Host code cannot
+// use the symbol itself as a device address, so that set-up looks the
+// address up once per device, with the device current, and caches it; a
+// cudaDeviceReset in between invalidates the cached address (a process that
+// resets a device must not call this entry point afterwards).
 #include <mutex>
 #include <string>
 
@@ -54,7 +59,7 @@ struct CurrentDevice {
 
 ct_status fail_cuda(cudaError_t e, const char *where) {
     ct_set_last_error((std::string(where) + ": " + cudaGetErrorString(e)).c_str());
-    return CT_ERR_CUDA;
+    return e == cudaErrorMemoryAllocation ? CT_ERR_ALLOC : CT_ERR_CUDA;
 }
 
 }  // namespace
@@ -76,7 +81,11 @@ extern "C" ct_status ct_fbp_fan_static_scratch(const ct_plan *plan, const float 
                               .c_str());
         return CT_ERR_WORKSPACE;
     }
-    if (ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024) return CT_ERR_UNSUPPORTED;
+    // the same width limit as ct_fbp_fan: only the direct filter's shared
+    // memory bounds the width; tensor-core plans take up to 4032 channels
+    if (plan->filter_algo != CT_FILTER_TOEPLITZ_TC &&
+        ctk::ramp_direct_smem(plan->g.n_cols) > 227 * 1024)
+        return CT_ERR_UNSUPPORTED;
     if (ctk::has_preweight(plan)) {
         ct_set_last_error("ct_fbp_fan_static_scratch: short-scan and cosine-weighted plans "
                           "need a second scratch sinogram; use ct_fbp_fan");

@@ -58,6 +58,39 @@ def ellipse_phantom(n: int, pixel_mm: float, seed: int, n_ellipses: int = 10,
     return rasterize(random_ellipses(rfov, seed, n_ellipses), n, ny, pixel_mm, pixel_mm)
 
 
+def ellipsoid_phantom(n: int, nz: int, pixel_mm: float, dz_mm: float, seed: int,
+                      n_ellipsoids: int = 12) -> np.ndarray:
+    """The seeded 3-D phantom of the cone workload, float32 [nz, n, n]: a water
+    cylinder (0.019/mm, radius 0.9*rFOV, 0.9 of the volume's height) plus
+    ``n_ellipsoids`` additive ellipsoids -- centres within 0.8*rFOV in x-y and
+    0.6 of the half-height in z, in-plane semi-axes in [0.05, 0.4]*rFOV, z
+    semi-axis in [0.1, 0.5] of the half-height, uniform rotation about z,
+    attenuation uniform in [-0.01, 0.03]/mm -- sampled at the voxel centres."""
+    rng = np.random.default_rng(seed)
+    rfov = n * pixel_mm / 2.0
+    hz = nz * dz_mm / 2.0
+    x = (np.arange(n) + 0.5) * pixel_mm - rfov
+    z = (np.arange(nz) + 0.5) * dz_mm - hz
+    X, Y = np.meshgrid(x, x)
+    vol = np.zeros((nz, n, n), np.float64)
+    cyl = (X ** 2 + Y ** 2 <= (0.9 * rfov) ** 2)
+    vol[np.abs(z) <= 0.9 * hz] += WATER_MU * cyl
+    for _ in range(n_ellipsoids):
+        r = 0.8 * rfov * math.sqrt(rng.uniform())
+        phi = rng.uniform(0.0, 2.0 * math.pi)
+        cx, cy = r * math.cos(phi), r * math.sin(phi)
+        cz = rng.uniform(-0.6, 0.6) * hz
+        a, b = rng.uniform(0.05 * rfov, 0.4 * rfov, size=2)
+        c = rng.uniform(0.1, 0.5) * hz
+        th = rng.uniform(0.0, math.pi)
+        mu = rng.uniform(-0.01, 0.03)
+        cs, sn = math.cos(th), math.sin(th)
+        q = (((X - cx) * cs + (Y - cy) * sn) / a) ** 2 + ((-(X - cx) * sn + (Y - cy) * cs) / b) ** 2
+        for k in np.nonzero(np.abs(z - cz) <= c)[0]:
+            vol[k] += mu * (q + ((z[k] - cz) / c) ** 2 <= 1.0)
+    return vol.astype(np.float32)
+
+
 def phantom_batch(batch: int, n: int, pixel_mm: float, seed0: int = 0) -> np.ndarray:
     """float32 [batch, n, n] with seeds seed0 .. seed0+batch-1."""
     return np.stack([ellipse_phantom(n, pixel_mm, seed0 + b) for b in range(batch)])

@@ -157,6 +157,38 @@ const char *ct_last_error(void);
 /* Number of kernels this library has launched in this process. */
 uint64_t ct_launch_count(void);
 
+/* ---- device memory ----------------------------------------------------------- */
+
+/* A caller-supplied device allocator.  The library takes device memory in
+ * exactly two places: the tables of a plan (ct_plan_create*, given back by
+ * ct_plan_destroy) and the scratch of an operator called with d_work == NULL
+ * (given back after the call's last kernel is enqueued).  The reference
+ * instead malloc'ed and freed its buffers inside every call and exited the
+ * process when one failed (FP/transform.cu:198-217, checkCudaErrors).
+ *   alloc(ctx, bytes, stream): device memory for work that will be enqueued
+ *     on `stream` (NULL for plan tables); NULL on failure, which the call
+ *     reports as CT_ERR_ALLOC after releasing what it already took.
+ *   free(ctx, ptr, stream): ptr is no longer needed once the work already
+ *     enqueued on `stream` has run (stream-ordered, as cudaFreeAsync); for
+ *     plan tables stream is NULL and the plan's work must have finished. */
+typedef struct ct_allocator {
+    void *ctx;
+    void *(*alloc)(void *ctx, size_t bytes, ct_stream stream);
+    void (*free)(void *ctx, void *ptr, ct_stream stream);
+} ct_allocator;
+
+/* Installs `allocator` for all later allocations of this process (a copy is
+ * kept; plans remember the allocator they were created with and give their
+ * tables back to it).  NULL restores the CUDA runtime (cudaMalloc for plan
+ * tables, cudaMallocAsync / cudaFreeAsync for scratch).  alloc and free must
+ * both be set.  Not synchronised with calls in flight on other threads: set
+ * it at start-up.  No counterpart in the reference. */
+ct_status ct_set_allocator(const ct_allocator *allocator);
+
+/* Number of device allocations this library has made in this process, by
+ * either route (ct_set_allocator's or the CUDA runtime's). */
+uint64_t ct_device_alloc_count(void);
+
 /* ---- geometry ------------------------------------------------------------ */
 
 /* Decodes the 16-float parameter vector.  Replaces the attr decoding of
@@ -405,13 +437,20 @@ ct_status ct_batch_set_config(const ct_batch_item *items, int n, const ct_batch_
  * and has no latency bound).  It calls no cudaMalloc, cudaMallocAsync,
  * cudaFree or allocating library routine; the filtered sinogram lives in a
  * fixed array of CT_FBP_STATIC_SCRATCH_FLOATS floats inside this library's
- * device code, which every GPU that loads the library holds until the process
- * exits.  The caller still passes the input and output buffers.
+ * device code, which every GPU it has been set up on (below) holds until the
+ * process exits.  The caller still passes the input and output buffers.
  *   - batch * n_views * n_cols above the capacity returns CT_ERR_WORKSPACE
  *     (ct_last_error says by how much); split the batch.
- *   - The first call on each device looks up the array's device address with
- *     that device current (cudaGetSymbolAddress) and caches it; make that
- *     first call before capturing any stream into a CUDA graph.
+ *   - The first call on each device is its set-up: it loads this part of
+ *     the library's device code on that device, which reserves the array
+ *     (the CUDA runtime loads device code lazily), and looks up and caches
+ *     the array's device address with that device current.  That call can
+ *     therefore fail with CT_ERR_ALLOC on a full device; make it once at
+ *     start-up (a warm-up call, e.g. with a small batch), before any device
+ *     memory is handed to the host framework and before capturing any
+ *     stream into a CUDA graph.  Later calls reserve nothing.  A
+ *     cudaDeviceReset invalidates the cached address: do not call this entry
+ *     point after resetting a device.
  *   - All calls on a device share the one array, which keeps the last call's
  *     contents (each call overwrites all it reads, so nothing needs clearing).
  *     Calls whose work overlaps on the GPU -- on different streams, or from
