@@ -362,12 +362,14 @@ def oracle_errors(dev, plan, plan_sl, imgs, usinos) -> dict:
     def dot(u_, v_):
         return float((u_.double() * v_.double()).sum())
 
-    l_, r_ = dot(plan.fp(xs), ys), dot(xs, plan.fp_adjoint(ys))
-    dots = {"fp_batch32": abs(l_ - r_) / abs(l_)}
-    l_, r_ = dot(plan_sl.fbp(ys), xs), dot(ys, plan_sl.fbp_adjoint(xs))
-    dots["fbp_batch32"] = abs(l_ - r_) / abs(l_)
-    l_, r_ = dot(plan.bp(ys), xs), dot(ys, plan.bp_adjoint(xs))
-    dots["bp_batch32"] = abs(l_ - r_) / abs(l_)
+    def mismatch(ax, y_, x_, aty):
+        """|<Ax, y> - <x, A^T y>| / (||Ax|| ||y||), as the tests define it."""
+        return abs(dot(ax, y_) - dot(x_, aty)) / (float(ax.double().norm()) *
+                                                  float(y_.double().norm()))
+
+    dots = {"fp_batch32": mismatch(plan.fp(xs), ys, xs, plan.fp_adjoint(ys)),
+            "fbp_batch32": mismatch(plan_sl.fbp_adjoint(xs), ys, xs, plan_sl.fbp(ys)),
+            "bp_batch32": mismatch(plan.bp_adjoint(xs), ys, xs, plan.bp(ys))}
     del xs, ys
 
     # uneven BF16 batch: one slice of each of the three geometries, FP / FBP / FBP adjoint
@@ -419,8 +421,8 @@ def oracle_errors(dev, plan, plan_sl, imgs, usinos) -> dict:
         "views": f"{nvc} of 984 (every {VIEWS // nvc}th)",
     }
     yc = torch.randn((1, nvc, 64, COLS), device=dev, generator=gen)
-    l_, r_ = dot(cplan.fdk(yc), vol), dot(yc, cplan.fdk_adjoint(vol))
-    dots["fdk_cone"] = abs(l_ - r_) / abs(l_)
+    vr = torch.randn((1, 64, N_PIX, N_PIX), device=dev, generator=gen)
+    dots["fdk_cone"] = mismatch(cplan.fdk_adjoint(vr), yc, vr, cplan.fdk(yc))
     cplan.close()
     out["dot_mismatch"] = dots
     f32 = [v for d in (c1, out["cone_512x512x64_888x64"]) for v in d.values()

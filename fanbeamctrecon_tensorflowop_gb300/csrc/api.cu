@@ -145,6 +145,13 @@ size_t fdk_cone_work_offset(const ct_plan *p, int batch) {
     return (copies * proj_bytes(p, batch) + 255) & ~(size_t)255;
 }
 
+// where the FBP adjoint's transpose work starts (after its sinogram
+// copies, 256-byte aligned)
+size_t fbp_adjoint_work_offset(const ct_plan *p, int batch) {
+    const size_t copies = ctk::has_preweight(p) ? 2 : 1;
+    return (copies * sino_bytes(p, batch) + 255) & ~(size_t)255;
+}
+
 // where the FDK adjoint's transpose work starts (after its projection
 // copies, 256-byte aligned)
 size_t fdk_adjoint_work_offset(const ct_plan *p, int batch) {
@@ -168,8 +175,10 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
         case CT_OP_FBP:  // + the backprojection's tap images
         case CT_OP_FDK_BP:
             return fbp_work_offset(p, batch) + ctk::bp_fan_work_bytes(p, batch);
-        case CT_OP_FBP_ADJOINT:
-            return parker * sino_bytes(p, batch);
+        case CT_OP_FBP_ADJOINT:  // + the transpose's slice-quad images
+            return fbp_adjoint_work_offset(p, batch) + ctk::bp_fan_transpose_work_bytes(p, batch);
+        case CT_OP_BP_ADJOINT:
+            return ctk::bp_fan_transpose_work_bytes(p, batch);
         default:
             return 0;
     }
@@ -180,7 +189,9 @@ void free_plan(ct_plan *p) {
     for (void *t : {(void *)p->d_view_cs, (void *)p->d_ray, (void *)p->d_ray_inv,
                     (void *)p->d_nsamp, (void *)p->d_taps, (void *)p->d_chan_s,
                     (void *)p->d_tc_hi, (void *)p->d_tc_lo, (void *)p->d_err,
-                    (void *)p->d_parker, (void *)p->d_cosw, (void *)p->d_view_z})
+                    (void *)p->d_parker, (void *)p->d_cosw, (void *)p->d_view_z,
+                    (void *)p->d_bpt_warp, (void *)p->d_bpt_bnd, (void *)p->d_bpt_ray,
+                    (void *)p->d_fov_row, (void *)p->d_fov_col})
         dev_free(p->alloc, t, nullptr, false);
     delete p;
 }
@@ -318,6 +329,8 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
     if (o.short_scan) ct_build_parker(geom, angles, &t);
     if (o.cosine_weight) ct_build_cosine(geom, n_rows, cone, &t);
     if (source_z) t.view_z.assign(source_z, source_z + n_angles);
+    ct_bpt_tables bt;
+    if (!cone) ct_build_bpt_tables(geom, angles, &bt);
 
     ct_plan *p = new (std::nothrow) ct_plan();
     if (!p) return CT_ERR_ALLOC;
@@ -380,6 +393,17 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
         ctk::build_tc_taps(t.taps.data(), geom->n_cols, hi, lo);
         if ((st = upload(p, &p->d_tc_hi, hi)) != CT_OK ||
             (st = upload(p, &p->d_tc_lo, lo)) != CT_OK) {
+            free_plan(p);
+            return st;
+        }
+    }
+    if (bt.ok) {
+        p->bpt_W = bt.W;
+        if ((st = upload(p, &p->d_bpt_warp, bt.warp)) != CT_OK ||
+            (st = upload(p, &p->d_bpt_bnd, bt.bnd)) != CT_OK ||
+            (st = upload(p, &p->d_bpt_ray, bt.ray)) != CT_OK ||
+            (st = upload(p, &p->d_fov_row, bt.fov_row)) != CT_OK ||
+            (st = upload(p, &p->d_fov_col, bt.fov_col)) != CT_OK) {
             free_plan(p);
             return st;
         }
@@ -507,7 +531,10 @@ ct_status ct_bp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_si
     if (st != CT_OK || batch == 0) return st;
     DeviceScope ds(plan->device);
     if (ds.err != cudaSuccess) return cuda_status(ds.err, "cudaSetDevice");
-    return launch_status(ctk::bp_fan_transpose(plan, d_img, d_sino, batch, 0, stream),
+    Workspace w;
+    st = acquire(w, nullptr, 0, op_workspace(plan, CT_OP_BP_ADJOINT, batch), stream);
+    if (st != CT_OK) return st;
+    return launch_status(ctk::bp_fan_transpose(plan, d_img, d_sino, batch, 0, w.ptr, stream),
                          "ct_bp_fan_adjoint");
 }
 
@@ -548,7 +575,10 @@ ct_status ct_fbp_fan_adjoint(const ct_plan *plan, const float *d_img, float *d_s
     st = acquire(w, d_work, work_bytes, op_workspace(plan, CT_OP_FBP_ADJOINT, batch), stream);
     if (st != CT_OK) return st;
     float *tmp = static_cast<float *>(w.ptr);
-    st = launch_status(ctk::bp_fan_transpose(plan, d_img, tmp, batch, 1, stream),
+    void *twork = ctk::bp_fan_transpose_work_bytes(plan, batch)
+                      ? static_cast<char *>(w.ptr) + fbp_adjoint_work_offset(plan, batch)
+                      : nullptr;
+    st = launch_status(ctk::bp_fan_transpose(plan, d_img, tmp, batch, 1, twork, stream),
                        "ct_fbp_fan_adjoint");
     if (st != CT_OK) return st;
     // The row filter is a symmetric Toeplitz matrix: its transpose is itself;

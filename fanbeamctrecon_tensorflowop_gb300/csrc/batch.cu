@@ -285,12 +285,17 @@ struct Layout {
     // per slice group: gathered inputs, results before the scatter, and the
     // plan path's workspace (all FP32, slices contiguous)
     std::vector<size_t> g_in, g_out, g_work;
+    // slice-quad images of the single FBP-adjoint items' transposes (they run
+    // one after another on the stream, so they share one buffer); SIZE_MAX
+    // when none uses the gather form
+    size_t tquads = SIZE_MAX;
     size_t total = 0;
 };
 constexpr size_t kCounterBytes = 256;
 
-// Where an FBP slice group's tap images start in its workspace (after the
-// filtered and pre-weighted sinograms, 256-byte aligned).
+// Where an FBP slice group's tap images (an FBP-adjoint group's slice-quad
+// images) start in its workspace (after the filtered and pre-weighted
+// sinograms, 256-byte aligned).
 size_t group_pairs_offset(const ct_batch_item &it, int g) {
     const ct_plan *p = it.plan;
     const size_t sino = sizeof(float) * (size_t)g * p->g.n_views * p->g.n_cols;
@@ -300,7 +305,6 @@ size_t group_pairs_offset(const ct_batch_item &it, int g) {
 // Workspace of a slice group's plan path.
 size_t group_work_bytes(const ct_batch_item &it, int g) {
     const ct_plan *p = it.plan;
-    const size_t sino = sizeof(float) * (size_t)g * p->g.n_views * p->g.n_cols;
     switch (it.op) {
         case CT_OP_FP:
             return fp_fan_work_bytes(p, g);
@@ -308,8 +312,8 @@ size_t group_work_bytes(const ct_batch_item &it, int g) {
             return bp_fan_work_bytes(p, g);
         case CT_OP_FBP:  // filtered (+ pre-weighted) sinograms, then tap images
             return group_pairs_offset(it, g) + bp_fan_work_bytes(p, g);
-        case CT_OP_FBP_ADJOINT:  // transposed (+ filtered) sinograms
-            return (has_preweight(p) ? 2 : 1) * sino;
+        case CT_OP_FBP_ADJOINT:  // transposed (+ filtered) sinograms, then slice quads
+            return group_pairs_offset(it, g) + bp_fan_transpose_work_bytes(p, g);
         default:
             return 0;
     }
@@ -363,6 +367,13 @@ Layout plan_layout(const ct_batch_item *items, int n, const Groups &G) {
                 break;
         }
     }
+    size_t tq = 0;
+    for (int i = 0; i < n; ++i)
+        if (G.group_of[(size_t)i] < 0 && items[i].op == CT_OP_FBP_ADJOINT) {
+            const size_t b = bp_fan_transpose_work_bytes(items[i].plan, 1);
+            tq = b > tq ? b : tq;
+        }
+    if (tq) L.tquads = take(tq);
     L.total = off;
     return L;
 }
@@ -494,7 +505,11 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
                                : nullptr;
                 if (r == 0) r = bp_fan(p, wk, out, g, 1, pw, s);
             } else {  // CT_OP_FBP_ADJOINT, as ct_fbp_fan_adjoint
-                r = bp_fan_transpose(p, in, wk, g, 1, s);
+                void *tw = bp_fan_transpose_work_bytes(p, g)
+                               ? static_cast<char *>(static_cast<void *>(wk)) +
+                                     group_pairs_offset(f, g)
+                               : nullptr;
+                r = bp_fan_transpose(p, in, wk, g, 1, tw, s);
                 if (r == 0 && !has_preweight(p)) {
                     r = ramp_filter(p, wk, out, rows, s);
                 } else if (r == 0) {
@@ -593,7 +608,10 @@ int batch_run(const ct_batch_item *items, int n, void *work, void *stream,
                 return (int)e;
         } else if (items[i].op == CT_OP_FBP_ADJOINT) {
             float *t = static_cast<float *>(at(L.filt[i]));
-            if ((e = (cudaError_t)bp_fan_transpose(p, in32, t, 1, 1, s)) != cudaSuccess)
+            void *tw = bp_fan_transpose_work_bytes(p, 1) && L.tquads != SIZE_MAX
+                           ? at(L.tquads)
+                           : nullptr;
+            if ((e = (cudaError_t)bp_fan_transpose(p, in32, t, 1, 1, tw, s)) != cudaSuccess)
                 return (int)e;
             float *dst = bf ? static_cast<float *>(at(L.out32[i]))
                             : static_cast<float *>(items[i].d_out);

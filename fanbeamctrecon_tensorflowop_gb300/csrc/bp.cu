@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Transpose of bp_fan_kernel: each pixel-view scatters x * weight * (1-f, f)
+// Transpose of bp_fan_kernel in scatter form (plans with texture weights, or
+// without a workspace): each pixel-view scatters x * weight * (1-f, f)
 // onto the two clamped detector taps with global atomics (L2 reductions).  A
 // thread evaluates each pixel-view's geometry once for GSB slices.
 // Atomics of one warp instruction that hit the same address serialise, so the
@@ -299,8 +300,17 @@ int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weigh
     return (int)cudaGetLastError();
 }
 
+size_t bp_fan_transpose_work_bytes(const ct_plan *p, int batch) {
+    return bp_gather_work_bytes(p, batch);
+}
+
+// The gather form (bp_gather.cu) where the plan has its tables, the
+// exact-weight interpolation and a workspace; otherwise the scatter below
+// (texture-weight plans keep it: it repeats the forward's own column
+// arithmetic, so the adjoint stays the exact transpose of those weights).
 int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch, int weighted,
-                     void *stream) {
+                     void *work, void *stream) {
+    if (work && bp_gather_usable(p)) return bp_gather(p, img, sino, batch, weighted, work, stream);
     const BpArgs a = make_args(p);
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
     cudaStream_t s = (cudaStream_t)stream;

@@ -331,3 +331,136 @@ void ct_build_parker(const ct_fan_geom *g, const float *angles, ct_host_tables *
         }
     }
 }
+
+// Tables of the gather-form BP transpose (bp_gather.cu).  For view v the
+// detector columns are cut into strips between boundary rays: strip b holds
+// the pixels whose column coordinate y = col + 1/2 lies in [b, b+1) -- the
+// pixels whose two clamped taps are (max(b-1, 0), min(b, C-1)) -- with the
+// outer strips cut at y = 1/2 and y = C + 1/2, where the backprojector's test
+// 0 < col < C ends (BP/transform.cu:88).  Boundary y = B lies on the ray
+// from the source at fan angle gamma = left + (B - shift - 1/2) dcol.  A warp
+// takes 32 consecutive strips (31 new per warp, channel group k: strips
+// 31k .. 31k+31) and walks the image lines across its rays: rows when the
+// rays run more along y, columns otherwise.  Per line the strip's pixels
+// lie between the two boundary rays' crossings of the line, and per pixel
+// the fraction f = (gamma_p - gamma_b)/dcol follows from the pixel's offset
+// from the lower boundary's crossing (exact, in 32.32 fixed point along the
+// line), never from the absolute column coordinate, whose FP32 rounding the
+// ramp filter of the FBP adjoint would amplify.
+void ct_build_bpt_tables(const ct_fan_geom *g, const float *angles, ct_bpt_tables *t) {
+    const int V = g->n_views, C = g->n_cols;
+    const int W = (C + kBptOut - 1) / kBptOut;
+    t->W = W;
+    t->ok = true;
+    t->warp.assign((size_t)V * W * 4, 0);
+    t->bnd.assign((size_t)V * W * 33 * 2, 0);
+    t->ray.assign((size_t)V * W * 32 * 4, 0.0f);
+    const double R = g->sid, dcol = g->dcol, left = g->left, shift = g->shift;
+    const double dx = g->dx, dy = g->dy, xmin = g->xmin, ymin = g->ymin;
+    const double r2 = (double)g->rfov * (double)g->rfov;
+    // per line, the inclusive pixel range inside the FOV disc (the
+    // backprojectors' own double-precision test)
+    t->fov_row.assign((size_t)g->ny * 2, 0);
+    t->fov_col.assign((size_t)g->nx * 2, 0);
+    for (int pass = 0; pass < 2; ++pass) {
+        const int nl = pass ? g->nx : g->ny, np = pass ? g->ny : g->nx;
+        std::vector<int32_t> &f = pass ? t->fov_col : t->fov_row;
+        for (int l = 0; l < nl; ++l) {
+            int lo = np, hi = -1;
+            for (int q = 0; q < np; ++q) {
+                const int ix = pass ? l : q, iy = pass ? q : l;
+                const double xd = xmin + dx * (ix + 0.5), yd = ymin + dy * (iy + 0.5);
+                if (xd * xd + yd * yd <= r2) {
+                    lo = q < lo ? q : lo;
+                    hi = q;
+                }
+            }
+            f[2 * (size_t)l] = lo;
+            f[2 * (size_t)l + 1] = hi;
+        }
+    }
+    const double rlim = (double)g->rfov + 2.0 * (dx > dy ? dx : dy);
+    const double two32 = 4294967296.0;
+    for (int v = 0; v < V; ++v) {
+        const double beta = (double)angles[v];
+        const double c = -std::cos(beta), s = -std::sin(beta);
+        const double Sx = -R * c, Sy = -R * s;  // the source; e_u = (c, s), e_t = (-s, c)
+        for (int k = 0; k < W; ++k) {
+            double d[33][2], n[33][2];
+            int along_y = 0, valid = 0;
+            for (int q = 0; q < 33; ++q) {
+                const int b = k * kBptOut + q;
+                const double B = b <= 0 ? 0.5 : (b >= C + 1 ? C + 0.5 : (double)b);
+                const double gam = left + (B - shift - 0.5) * dcol;
+                const double cg = std::cos(gam), sg = std::sin(gam);
+                d[q][0] = cg * c - sg * s;
+                d[q][1] = cg * s + sg * c;
+                n[q][0] = -sg * c - cg * s;
+                n[q][1] = -sg * s + cg * c;
+                if (b <= C + 1) {
+                    ++valid;
+                    along_y += std::fabs(d[q][1]) >= std::fabs(d[q][0]);
+                }
+            }
+            const int layout = 2 * along_y >= valid ? 0 : 1;  // 0: walk rows, 1: walk columns
+            const int aw = layout ? 0 : 1, ap = 1 - aw;         // walk / pixel axis components
+            const double lmin = layout ? xmin : ymin, dl = layout ? dx : dy;
+            const double pmin = layout ? ymin : xmin, dp = layout ? dy : dx;
+            const double Sw = layout ? Sx : Sy, Sp = layout ? Sy : Sx;
+            const int nlines = layout ? g->nx : g->ny;
+            int orient = 0;
+            double jmin = 1e300, jmax = -1e300;
+            for (int q = 0; q < 33; ++q) {
+                if (k * kBptOut + q > C + 1) break;
+                if (std::fabs(d[q][aw]) < 0.2) t->ok = false;
+                const int o = n[q][ap] > 0.0 ? 1 : -1;
+                if (orient && o != orient) t->ok = false;
+                orient = o;
+                // the ray's chord of the FOV disc (widened), in line indices
+                const double dist = std::fabs(Sx * d[q][1] - Sy * d[q][0]);
+                if (dist < rlim) {
+                    const double lm = -(Sx * d[q][0] + Sy * d[q][1]);
+                    const double h = std::sqrt(rlim * rlim - dist * dist);
+                    for (double L : {lm - h, lm + h}) {
+                        const double w = Sw + L * d[q][aw];
+                        const double jl = (w - lmin) / dl - 0.5;
+                        jmin = jl < jmin ? jl : jmin;
+                        jmax = jl > jmax ? jl : jmax;
+                    }
+                }
+            }
+            int J0 = 1, J1 = 0;
+            if (jmax >= jmin) {
+                J0 = (int)std::floor(jmin) - 2;
+                J1 = (int)std::ceil(jmax) + 2;
+                J0 = J0 < 0 ? 0 : J0;
+                J1 = J1 > nlines - 1 ? nlines - 1 : J1;
+            }
+            const size_t e = (size_t)v * W + k;
+            t->warp[4 * e] = layout | (orient > 0 ? 2 : 0);
+            t->warp[4 * e + 1] = J0;
+            t->warp[4 * e + 2] = J1;
+            const double wl = lmin + dl * (J0 + 0.5);  // line J0's coordinate
+            for (int q = 0; q < 33; ++q) {
+                const double dw = std::fabs(d[q][aw]) < 1e-12 ? 1e-12 : d[q][aw];
+                const double L0 = (wl - Sw) / dw;  // along the ray to line J0
+                const double X0 = (Sp + L0 * d[q][ap] - pmin) / dp - 0.5;
+                const double step = dl / dw * d[q][ap] / dp;
+                const double lim = 4.0e9;  // far beyond any image: clamp, the range is then empty
+                auto fx = [&](double x) {
+                    x = x > lim ? lim : (x < -lim ? -lim : x);
+                    return (int64_t)std::llround(x * two32);
+                };
+                t->bnd[2 * (e * 33 + q)] = fx(X0);
+                t->bnd[2 * (e * 33 + q) + 1] = fx(step);
+                if (q < 32) {
+                    float *r = &t->ray[4 * (e * 32 + q)];
+                    r[0] = (float)L0;
+                    r[1] = (float)(dl / dw);
+                    r[2] = (float)(dp * n[q][ap]);
+                    r[3] = (float)(dp * d[q][ap]);
+                }
+            }
+        }
+    }
+}

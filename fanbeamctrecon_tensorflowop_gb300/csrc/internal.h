@@ -35,7 +35,22 @@ struct ct_host_tables {
     double total_samples = 0;        // sum of nsamp over all rays
 };
 
+// Gather-form BP transpose (bp_gather.cu): per view, channel groups of
+// kBptOut output channels (32 strips per warp), boundary rays in 32.32 fixed
+// point along the image lines the warp walks.
+constexpr int kBptOut = 31;
+struct ct_bpt_tables {
+    int W = 0;                        // channel groups per view
+    bool ok = false;                  // false: a ray of some group runs along its lines
+    std::vector<int32_t> warp;        // [V][W][4]: layout | orient << 1, first line, last line, 0
+    std::vector<int64_t> bnd;         // [V][W][33][2]: crossing of the first line, step per line
+    std::vector<float> ray;           // [V][W][32][4]: L at the first line, dL per line, na, da
+    std::vector<int32_t> fov_row;     // [ny][2]: pixels of row j inside the FOV (inclusive)
+    std::vector<int32_t> fov_col;     // [nx][2]: pixels of column i inside the FOV
+};
+
 // geometry.cpp
+void ct_build_bpt_tables(const ct_fan_geom *g, const float *angles, ct_bpt_tables *t);
 ct_status ct_decode_param16(const float p[16], ct_fan_geom *g);
 ct_status ct_validate_geom(const ct_fan_geom *g);
 void ct_build_view_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t);
@@ -80,6 +95,12 @@ struct ct_plan {
     float *d_parker;                 // [V*C] short-scan weights, or NULL (full scan)
     float *d_cosw;                   // [n_rows*C] cosine pre-weights, or NULL
     float *d_view_z;                 // [V] source heights (mm), or NULL (orbit at z = 0)
+    // gather-form BP transpose (fan plans whose ct_bpt_tables are ok), else NULL
+    int bpt_W;
+    int32_t *d_bpt_warp;             // [V][W] int4
+    int64_t *d_bpt_bnd;              // [V][W][33] longlong2
+    float *d_bpt_ray;                // [V][W][32] float4
+    int32_t *d_fov_row, *d_fov_col;  // [ny] int2, [nx] int2
 };
 
 // Kernel launchers (defined in the .cu files).  Each returns the launch error.
@@ -99,8 +120,17 @@ int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, v
 size_t bp_fan_work_bytes(const ct_plan *p, int batch);
 int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weighted, void *work,
            void *stream);
+// work: bp_fan_transpose_work_bytes(p, batch) bytes (slice-quad images of up
+// to 64 slices in both layouts) for the gather form; NULL, or a plan without
+// its tables or with texture weights, takes the atomic scatter form
+size_t bp_fan_transpose_work_bytes(const ct_plan *p, int batch);
+// bp_gather.cu: the gather form (plans with the tables, exact weights)
+bool bp_gather_usable(const ct_plan *p);
+size_t bp_gather_work_bytes(const ct_plan *p, int batch);
+int bp_gather(const ct_plan *p, const float *img, float *sino, int batch, int weighted,
+              void *work, void *stream);
 int bp_fan_transpose(const ct_plan *p, const float *img, float *sino, int batch, int weighted,
-                     void *stream);
+                     void *work, void *stream);
 int ramp_filter(const ct_plan *p, const float *in, float *out, int rows, void *stream);
 size_t ramp_direct_smem(int C);
 int tc_padded(int C);

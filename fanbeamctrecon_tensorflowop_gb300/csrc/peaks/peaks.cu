@@ -22,6 +22,17 @@ namespace {
 constexpr int kL1Bytes = 32 * 1024;  // per-SM working set: well inside L1
 constexpr int kL1Vec = kL1Bytes / 16;
 
+__device__ __forceinline__ float4 ld_nc(const float4 *p) {
+    float4 v;
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+// Each iteration a warp reads 8 x 512 contiguous bytes; the window moves by
+// 32 float4 per iteration, so no load repeats an address of the previous
+// iteration (the volatile loads are never merged or hoisted either).
 __global__ void __launch_bounds__(512) l1_load_kernel(const float4 *__restrict__ buf, int iters,
                                                       float *__restrict__ sink) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -29,13 +40,13 @@ __global__ void __launch_bounds__(512) l1_load_kernel(const float4 *__restrict__
     for (int it = 0; it < iters; ++it) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const float4 v = __ldg(buf + ((idx + k * 512) & (kL1Vec - 1)));
+            const float4 v = ld_nc(buf + ((idx + k * 512) & (kL1Vec - 1)));
             acc.x += v.x;
             acc.y += v.y;
             acc.z += v.z;
             acc.w += v.w;
         }
-        idx = (idx + 8 * 512) & (kL1Vec - 1);
+        idx = (idx + 32) & (kL1Vec - 1);
     }
     // the buffer holds zeros: this store never happens, but the compiler
     // cannot know it, so every load stays

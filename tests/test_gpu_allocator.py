@@ -85,7 +85,7 @@ def test_every_allocation_goes_through_the_hook(cuda, lib):
     assert lib.ct_fp_fan(plan._h, x.data_ptr(), out.data_ptr(), 3, None, 0, stream) == 0
     torch.cuda.synchronize()
     assert fake.calls == tables + 1            # the call's scratch
-    assert fake.streams[-1] == stream          # on the call's stream
+    assert (fake.streams[-1] or 0) == stream   # on the call's stream (0: the legacy default)
     assert fake.freed == 1 and len(fake.live) == tables
     assert lib.ct_device_alloc_count() - n0 == fake.calls
     # same result as with caller-provided scratch

@@ -17,9 +17,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _tol(op):
-    # the FBP adjoint's weighted-BP transpose adds with float atomics, so its
-    # summation order (and last bits) vary from run to run
-    return 1e-5 if op == "fbp_adjoint" else 1e-6
+    return 1e-6
 
 
 def _np(t):

@@ -55,6 +55,27 @@ def test_fp_adjoint_clinical_against_oracle(cuda, orc, c1):
     assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
 
 
+@pytest.mark.parametrize("window", ["ramlak", "shepp_logan"])
+def test_bp_and_fbp_adjoint_clinical_against_oracle(cuda, orc, c1, window):
+    """The BP transpose and the FBP adjoint at 512^2 / 984 x 888 on the seeded
+    phantom.  The FBP adjoint ends with the ramp filter, which amplifies the
+    transpose's per-pixel column errors about 80-fold: the gather form keeps
+    them at ~1e-7 of a channel."""
+    from fanbeamctrecon_tensorflowop_gb300 import _lib
+    p, a, plan, g = c1
+    win = _lib.WINDOW_SHEPP_LOGAN if window == "shepp_logan" else _lib.WINDOW_RAMLAK
+    plan_w = FanPlan(p, a, device=cuda, window=win)
+    x = phantom.phantom_batch(2, 512, 0.7, seed0=4)
+    got = _np(plan_w.fbp_adjoint(_t(x, cuda)))
+    ref = orc.fbp_fan_adjoint(g, a, x[:1], window=orc.SHEPP_LOGAN if window == "shepp_logan"
+                              else orc.RAMLAK)
+    assert rel_l2(got[:1], ref) <= TOL, rel_l2(got[:1], ref)
+    if window == "ramlak":
+        got = _np(plan.bp_adjoint(_t(x, cuda)))
+        ref = orc.bp_fan_transpose(g, a, x[1:2])
+        assert rel_l2(got[1:2], ref) <= TOL, rel_l2(got[1:2], ref)
+
+
 def test_batch32_gradient_clinical(cuda, orc, c1):
     """Config 2: batch of 32 clinical slices, y = FP(phantom) + N(0, (0.01 max)^2)."""
     from fanbeamctrecon_tensorflowop_gb300.autograd import forward_project
@@ -121,6 +142,7 @@ def test_cone_clinical_dot(cuda, c4):
     gen = torch.Generator(device=cuda).manual_seed(2)
     x = torch.randn((1, *plan.volume_shape), device=cuda, generator=gen)
     y = torch.randn((1, *plan.proj_shape), device=cuda, generator=gen)
-    l_ = float((plan.fdk(y).double() * x.double()).sum())
-    r_ = float((y.double() * plan.fdk_adjoint(x).double()).sum())
-    assert abs(l_ - r_) / abs(l_) <= DOT_TOL
+    ax, aty = plan.fdk_adjoint(x).double(), plan.fdk(y).double()
+    m = abs(float((ax * y.double()).sum()) - float((x.double() * aty).sum())) / (
+        float(ax.norm()) * float(y.double().norm()))
+    assert m <= DOT_TOL, m
