@@ -501,9 +501,16 @@ def main() -> None:
     ap.add_argument("--views", type=int, default=VIEWS, help="--profile-case: views")
     ap.add_argument("--n", type=int, default=N_PIX, help="--profile-case: image size")
     ap.add_argument("--window", default="ramlak", choices=["ramlak", "shepp_logan"])
+    ap.add_argument("--peaks-only", action="store_true",
+                    help="measure and print the L1-load and FP32 peaks, then exit")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)
+        return
+    if args.peaks_only:
+        import torch
+        torch.cuda.init()
+        print(json.dumps(measure_peaks(gpu_index_for_smi(int(os.environ.get("LOCAL_RANK", "0"))))))
         return
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

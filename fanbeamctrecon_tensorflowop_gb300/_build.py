@@ -54,8 +54,8 @@ def _headers() -> list[Path]:
     return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
-def _fingerprint() -> str:
-    h = hashlib.sha256()
+def _fingerprint(extra: str = "") -> str:
+    h = hashlib.sha256(extra.encode())
     for p in _sources() + _headers():
         h.update(p.name.encode())
         h.update(p.read_bytes())
@@ -65,13 +65,13 @@ def _fingerprint() -> str:
     return h.hexdigest()
 
 
-def _compile(src: Path) -> Path:
-    obj = BUILD_DIR / (src.name + ".o")
+def _compile(src: Path, out_dir: Path = BUILD_DIR, defines: tuple = ()) -> Path:
+    obj = out_dir / (src.name + ".o")
     if src.suffix == ".cu":
-        cmd = [_nvcc(), *NVCC_FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
+        cmd = [_nvcc(), *NVCC_FLAGS, *defines, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
     else:
-        cmd = ["g++", *CXX_FLAGS, "-I", str(INCLUDE), "-I", _cuda_include(), "-c", str(src),
-               "-o", str(obj)]
+        cmd = ["g++", *CXX_FLAGS, *defines, "-I", str(INCLUDE), "-I", _cuda_include(), "-c",
+               str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
@@ -80,8 +80,36 @@ def _compile(src: Path) -> Path:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compiles libctgb.so unless an up-to-date build is present; returns its path."""
+DEBUG_DIR = BUILD_DIR / "debug"
+
+
+def build_debug(force: bool = False) -> Path:
+    """The debug library (_build/debug/libctgb.so): the same sources with
+    -DCT_DEBUG, whose kernels check every gather index (see dbgcheck.cuh)."""
+    DEBUG_DIR.mkdir(parents=True, exist_ok=True)
+    stamp = DEBUG_DIR / "stamp.txt"
+    lib = DEBUG_DIR / LIB_NAME
+    fp = _fingerprint("debug")
+    if not force and lib.exists() and stamp.exists() and stamp.read_text() == fp:
+        return lib
+    srcs = _sources()
+    with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
+        objs = list(ex.map(lambda p: _compile(p, DEBUG_DIR, ("-DCT_DEBUG",)), srcs))
+    tmp = DEBUG_DIR / (LIB_NAME + ".tmp")
+    cmd = [_nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, lib)
+    stamp.write_text(fp)
+    return lib
+
+
+def build(force: bool = False, verbose: bool = False, debug: bool = False) -> Path:
+    """Compiles libctgb.so unless an up-to-date build is present; returns its
+    path.  debug=True builds (and returns) the index-checking debug library."""
+    if debug:
+        return build_debug(force)
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     stamp = BUILD_DIR / "stamp.txt"
     fp = _fingerprint()

@@ -15,7 +15,9 @@ CT_OK = 0
 STATUS_NAMES = {
     0: "CT_OK", 1: "CT_ERR_INVALID_ARGUMENT", 2: "CT_ERR_NULL_POINTER", 3: "CT_ERR_WORKSPACE",
     4: "CT_ERR_CUDA", 5: "CT_ERR_ALLOC", 6: "CT_ERR_UNSUPPORTED", 7: "CT_ERR_TIMEOUT",
+    8: "CT_ERR_DEVICE_CHECK",
 }
+BUILD_INDEX_CHECKS = 1  # ct_build_flags bit
 
 # ct_filter_window / ct_filter_algo / ct_op
 WINDOW_RAMLAK = 0
@@ -108,6 +110,7 @@ SIGNATURES = {
     "ct_version": (ctypes.c_char_p, []),
     "ct_last_error": (ctypes.c_char_p, []),
     "ct_launch_count": (ctypes.c_uint64, []),
+    "ct_build_flags": (ctypes.c_uint32, []),
     "ct_set_allocator": (_i, [_P(CtAllocator)]),
     "ct_device_alloc_count": (ctypes.c_uint64, []),
     "ct_geom_from_param16": (_i, [_P(ctypes.c_float), _P(CtFanGeom)]),
@@ -156,6 +159,15 @@ def lib_path() -> Path:
     return _build.LIB_PATH
 
 
+def _bind(path) -> ctypes.CDLL:
+    lib = ctypes.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
     """Loads libctgb.so (building it in-tree first if it is absent or stale)."""
     global _lib
@@ -165,13 +177,22 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         path = _build.build() if build_if_missing else _build.LIB_PATH
         if not Path(path).exists():
             raise RuntimeError(f"libctgb.so not found at {path}; run __graft_entry__.build()")
-        lib = ctypes.CDLL(str(path))
-        for name, (res, args) in SIGNATURES.items():
-            fn = getattr(lib, name)
-            fn.restype = res
-            fn.argtypes = args
-        _lib = lib
-        return lib
+        _lib = _bind(path)
+        return _lib
+
+
+_debug_lib = None
+
+
+def load_debug() -> ctypes.CDLL:
+    """The debug build of the library (kernels with index checks, -DCT_DEBUG),
+    built in-tree on first use into _build/debug/.  A separate library with
+    its own plans: pass it only plans it created."""
+    global _debug_lib
+    with _lock:
+        if _debug_lib is None:
+            _debug_lib = _bind(_build.build(debug=True))
+        return _debug_lib
 
 
 def check(status: int, where: str) -> None:

@@ -186,7 +186,8 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
 
 void free_plan(ct_plan *p) {
     if (!p) return;
-    for (void *t : {(void *)p->d_view_cs, (void *)p->d_ray, (void *)p->d_ray_inv,
+    for (void *t : {(void *)p->d_view_cs, (void *)p->d_view_cs_lo, (void *)p->d_col_tan,
+                    (void *)p->d_ray, (void *)p->d_ray_inv,
                     (void *)p->d_nsamp, (void *)p->d_taps, (void *)p->d_chan_s,
                     (void *)p->d_tc_hi, (void *)p->d_tc_lo, (void *)p->d_err,
                     (void *)p->d_parker, (void *)p->d_cosw, (void *)p->d_view_z,
@@ -235,6 +236,38 @@ ct_status filtered_bp(const ct_plan *p, const float *d_sino, float *d_img, int b
 
 void ct_count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+#ifdef CT_DEBUG
+namespace ctk {
+namespace dbg {
+namespace {
+struct FlagReader {
+    TakeFn fn;
+    const char *file;
+};
+std::vector<FlagReader> &registry() {
+    static std::vector<FlagReader> r;
+    return r;
+}
+}  // namespace
+void add_flag(TakeFn fn, const char *file) { registry().push_back(FlagReader{fn, file}); }
+}  // namespace dbg
+}  // namespace ctk
+
+// Reads and clears every file's index-check flag (debug builds); returns the
+// first raised one as "file:line" in *where, or false.
+static bool take_debug_flags(std::string *where) {
+    bool any = false;
+    for (const auto &r : ctk::dbg::registry()) {
+        const unsigned line = r.fn();
+        if (line && !any) {
+            *where = std::string(r.file) + ":" + std::to_string(line);
+            any = true;
+        }
+    }
+    return any;
+}
+#endif
+
 void ct_set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
 
 extern "C" {
@@ -249,6 +282,7 @@ const char *ct_status_string(ct_status s) {
         case CT_ERR_ALLOC: return "CT_ERR_ALLOC: allocation failed";
         case CT_ERR_UNSUPPORTED: return "CT_ERR_UNSUPPORTED: not supported by this build";
         case CT_ERR_TIMEOUT: return "CT_ERR_TIMEOUT: a bounded device wait gave up";
+        case CT_ERR_DEVICE_CHECK: return "CT_ERR_DEVICE_CHECK: a debug build's index check failed";
     }
     return "unknown ct_status";
 }
@@ -258,6 +292,8 @@ const char *ct_version(void) { return "ctgb 0.1.0 (sm_103a)"; }
 const char *ct_last_error(void) { return g_last_error.c_str(); }
 
 uint64_t ct_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+uint32_t ct_build_flags(void) { return CT_DEBUG_BUILD ? CT_BUILD_INDEX_CHECKS : 0u; }
 
 ct_status ct_set_allocator(const ct_allocator *allocator) {
     ct_allocator a{};
@@ -377,6 +413,8 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
         return cuda_status(e, "cudaGetDevice");
     }
     if ((st = upload(p, &p->d_view_cs, t.view_cs)) != CT_OK ||
+        (st = upload(p, &p->d_view_cs_lo, t.view_cs_lo)) != CT_OK ||
+        (st = upload(p, &p->d_col_tan, t.col_tan)) != CT_OK ||
         (st = upload(p, &p->d_ray, t.ray)) != CT_OK ||
         (st = upload(p, &p->d_nsamp, t.nsamp)) != CT_OK ||
         (st = upload(p, &p->d_ray_inv, ray_inv)) != CT_OK ||
@@ -460,6 +498,13 @@ ct_status ct_plan_check(const ct_plan *plan) {
         g_last_error = "a kernel's bounded wait gave up";
         return CT_ERR_TIMEOUT;
     }
+#ifdef CT_DEBUG
+    std::string where;
+    if (take_debug_flags(&where)) {
+        g_last_error = "index check failed at " + where;
+        return CT_ERR_DEVICE_CHECK;
+    }
+#endif
     return CT_OK;
 }
 

@@ -113,17 +113,19 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
                     float v0[SB], v1[SB];
                     if constexpr (PAIRS) {
                         const float4 *q = pairs + ((size_t)v * (a.C + 1) + i) * (SB / 2);
+                        const bool ok = (unsigned)i <= (unsigned)a.C;
 #pragma unroll
                         for (int h = 0; h < SB / 2; ++h) {
-                            const float4 t = __ldg(q + h);
+                            const float4 t = CT_DLOAD(ok, q + h);
                             v0[2 * h] = t.x, v1[2 * h] = t.y, v0[2 * h + 1] = t.z,
                                      v1[2 * h + 1] = t.w;
                         }
                     } else {
+                        const bool ok = (unsigned)i0 < (unsigned)a.C && (unsigned)i1 < (unsigned)a.C;
 #pragma unroll
                         for (int s = 0; s < SB; ++s) {
-                            v0[s] = __ldg(sb[s] + ro + i0);
-                            v1[s] = __ldg(sb[s] + ro + i1);
+                            v0[s] = CT_DLOAD(ok, sb[s] + ro + i0);
+                            v1[s] = CT_DLOAD(ok, sb[s] + ro + i1);
                         }
                     }
 #pragma unroll

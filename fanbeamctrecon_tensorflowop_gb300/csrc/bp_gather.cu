@@ -99,7 +99,9 @@ __global__ void __launch_bounds__(128)
             const float F = __uint2float_rn(fl) * 2.3283064365386963e-10f;  // 2^-32
             const float Lb = fmaf((float)t, rr.y, rr.x);
             const float4 *line = img + (size_t)j * npx;
+            const int nlines = colwalk ? a.nx : a.ny;
             for (int i = i0; i <= i1; ++i) {
+                const bool ok = (unsigned)i < (unsigned)npx && (unsigned)j < (unsigned)nlines;
                 const float dp = (float)(i - hl) - F;  // offset from the lower boundary (pixels)
                 const float n = dp * rr.z;              // normal distance (mm)
                 const float L = fmaf(dp, rr.w, Lb);     // distance along the boundary ray (mm)
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(128)
                 const unsigned long long pa = dup2(wa), pb = dup2(wb);
 #pragma unroll
                 for (int h = 0; h < NQ; ++h) {
-                    const float4 x = __ldg(line + h * qplane + i);
+                    const float4 x = CT_DLOAD(ok, line + h * qplane + i);
                     const unsigned long long x01 = pack2(x.x, x.y), x23 = pack2(x.z, x.w);
                     A[2 * h] = fma2(pa, x01, A[2 * h]);
                     A[2 * h + 1] = fma2(pa, x23, A[2 * h + 1]);

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "dbgcheck.cuh"
 #include "internal.h"
 
 namespace ctk {

@@ -12,6 +12,7 @@
 #include <climits>
 
 #include "cellwalk.cuh"
+#include "colprec.cuh"
 #include "fp_body.cuh"
 
 #ifndef CT_CONE_FP_ROWS
@@ -148,7 +149,9 @@ __global__ void __launch_bounds__(kThreads, CT_CONE_BP_MINB)
                 split_pos(rr, ir, fr);
                 float va0, va1, vc0, vc1;
                 if constexpr (QUAD) {
-                    const float4 t = __ldg(qv + (size_t)ir * (a.C + 1));
+                    const bool ok = (unsigned)ir <= (unsigned)a.n_rows &&
+                                    (unsigned)ic <= (unsigned)a.C;
+                    const float4 t = CT_DLOAD(ok, qv + (size_t)ir * (a.C + 1));
                     va0 = t.x;
                     va1 = t.y;
                     vc0 = t.z;
@@ -222,7 +225,9 @@ constexpr int kRB = 16;
 template <int DEG, bool TEX>
 __global__ void __launch_bounds__(kThreads)
     cone_bp_transpose_kernel(const float *__restrict__ vol, float *__restrict__ proj,
-                             const float2 *__restrict__ view_cs, const float *__restrict__ view_z,
+                             const float2 *__restrict__ view_cs,
+                             const float2 *__restrict__ view_cs_lo,
+                             const float2 *__restrict__ col_tan, const float *__restrict__ view_z,
                              const int *__restrict__ vmax_bits, ConeArgs a, int batch) {
     // [kRB][C] fixed point, then [2][C]: the first and the last detector row's
     // clamped samples, fixed point at their own scale
@@ -241,6 +246,7 @@ __global__ void __launch_bounds__(kThreads)
     const float scale_c = bound_c > 0.0f ? 1073741824.0f / bound_c : 0.0f;
     __syncthreads();
     const float2 cs = __ldg(view_cs + v);
+    const float2 csl = __ldg(view_cs_lo + v);
     const float zfirst = a.zmin + 0.5f * a.dz - (view_z ? __ldg(view_z + v) : 0.0f);
     const float *vb = vol + (size_t)b * a.nz * a.ny * a.nx;
     const float rmax = (float)a.n_rows;
@@ -270,7 +276,14 @@ __global__ void __launch_bounds__(kThreads)
         float f;
         split_pos(y, ic, f);
         const float A = floorf(fmaf(f, 256.0f, 0.5f));  // used with TEX only
-        if constexpr (TEX) f = A * (1.0f / 256.0f);
+        if constexpr (TEX) {
+            f = A * (1.0f / 256.0f);
+        } else {  // the column fraction from float-float geometry (colprec.cuh)
+            FF Uf, tf;
+            ff_ut(px, (float)(xd - (double)px), py, (float)(yd - (double)py), cs.x, csl.x, cs.y,
+                  csl.y, a.R, Uf, tf);
+            precise_strip(Uf, tf, col_tan, a.inv_dcol, a.C, ic, f);
+        }
         const int i0 = max(ic - 1, 0), i1 = min(ic, a.C - 1);
         const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
         const float slope = a.row_scale * rU;
@@ -405,12 +418,13 @@ __global__ void __launch_bounds__(256)
     if (tx == 0 && m > 0.0f) atomicMax(vmax_bits + b, __float_as_int(m));
 }
 
-// Per image row iy: the fp32 pixel centre py[iy] and the span [lo, hi) of
-// columns whose centres lie in the FOV disc (an interval: the test is
-// monotone in |x|); px[ix] likewise.  Same double expressions as
+// Per image row iy: the fp32 pixel centre py[iy] (and its rounding, pyl[iy])
+// and the span [lo, hi) of columns whose centres lie in the FOV disc (an
+// interval: the test is monotone in |x|); px[ix], pxl[ix] likewise.  Same double expressions as
 // cone_bp_kernel's FOV test, so both select the same pixels.
 __global__ void __launch_bounds__(32)
     cone_fov_tables_kernel(ConeArgs a, float *__restrict__ px_tab, float *__restrict__ py_tab,
+                           float *__restrict__ pxl_tab, float *__restrict__ pyl_tab,
                            int2 *__restrict__ span) {
     const int iy = blockIdx.x, lane = threadIdx.x;
     const double yd = (double)a.ymin + (double)a.dy * (iy + 0.5);
@@ -422,13 +436,17 @@ __global__ void __launch_bounds__(32)
             lo = min(lo, ix);
             hi = max(hi, ix);
         }
-        if (iy == 0 && ix < a.nx) px_tab[ix] = (float)xd;
+        if (iy == 0 && ix < a.nx) {
+            px_tab[ix] = (float)xd;
+            pxl_tab[ix] = (float)(xd - (double)(float)xd);
+        }
     }
     lo = __reduce_min_sync(0xffffffffu, lo);
     hi = __reduce_max_sync(0xffffffffu, hi);
     if (lane == 0) {
         span[iy] = hi >= 0 ? make_int2(lo, hi + 1) : make_int2(0, 0);
         py_tab[iy] = (float)yd;
+        pyl_tab[iy] = (float)(yd - (double)(float)yd);
     }
 }
 
@@ -479,8 +497,11 @@ template <int DEG, bool TEX>
 __global__ void __launch_bounds__(kZThreads, 1)
     cone_bp_transpose_z_kernel(const float *__restrict__ vol_t, float *__restrict__ proj,
                                const float2 *__restrict__ view_cs,
+                               const float2 *__restrict__ view_cs_lo,
+                               const float2 *__restrict__ col_tan,
                                const float *__restrict__ view_z, const int *__restrict__ vmax_bits,
                                const float *__restrict__ px_tab, const float *__restrict__ py_tab,
+                               const float *__restrict__ pxl_tab, const float *__restrict__ pyl_tab,
                                const int2 *__restrict__ span, ConeArgs a, int nzp, int lg) {
     extern __shared__ int4 acc4[];
     int *acc = reinterpret_cast<int *>(acc4);
@@ -495,6 +516,7 @@ __global__ void __launch_bounds__(kZThreads, 1)
     const float scale_c = bound_c > 0.0f ? 1073741824.0f / bound_c : 0.0f;
     __syncthreads();
     const float2 cs = __ldg(view_cs + v);
+    const float2 csl = __ldg(view_cs_lo + v);
     const float zs = view_z ? __ldg(view_z + v) : 0.0f;
     const float rmax = (float)a.n_rows;
     const int last = a.n_rows - 1;
@@ -537,15 +559,23 @@ __global__ void __launch_bounds__(kZThreads, 1)
                 float f;
                 split_pos(y, ic, f);
                 const float A = floorf(fmaf(f, 256.0f, 0.5f));  // used with TEX only
+                if constexpr (!TEX) {  // the column fraction from float-float geometry
+                    FF Uf, tf;
+                    ff_ut(px, __ldg(pxl_tab + ix), py, __ldg(pyl_tab + cur.iy), cs.x, csl.x, cs.y,
+                          csl.y, a.R, Uf, tf);
+                    precise_strip(Uf, tf, col_tan, a.inv_dcol, a.C, ic, f);
+                }
                 int *c0 = acc + max(ic - 1, 0) * ld;
                 int *c1 = acc + min(ic, a.C - 1) * ld;
                 const float wgt = __fdividef(1.0f, fmaf(U, U, t * t));
                 const float slope = a.row_scale * rU;
                 const float drr = a.dz * slope;
                 const unsigned long long g01 = zt_pack(1.0f - f, f);  // column weights
+                const bool cols_ok = (unsigned)ic <= (unsigned)a.C;
                 auto emit = [&](int row, unsigned long long X) {
                     const float sc = (unsigned)(row - 1) < (unsigned)(last - 1) ? scale : scale_c;
                     const float2 v = zt_unpack(zt_mul2(X, zt_pack(sc, sc)));
+                    if (!CT_DCHECK(cols_ok && (unsigned)row < (unsigned)a.n_rows)) return;
                     atomicAdd(c0 + row, __float2int_rn(v.x));
                     atomicAdd(c1 + row, __float2int_rn(v.y));
                 };
@@ -765,8 +795,9 @@ __global__ void __launch_bounds__(kConeFpThreads)
             const float cz = wk - kz, d = dw[rr];
             const int z0 = min(max((int)kz, 0), a.nz - 1);
             const int z1 = min(max((int)kz + 1, 0), a.nz - 1);
-            const float4 t0 = __ldg(qc + (size_t)z0 * sstride);
-            const float4 t1 = __ldg(qc + (size_t)z1 * sstride);
+            const bool ok = (unsigned)(cu + 1) < (unsigned)Q && (unsigned)(cv + 1) < (unsigned)Q;
+            const float4 t0 = CT_DLOAD(ok, qc + (size_t)z0 * sstride);
+            const float4 t1 = CT_DLOAD(ok, qc + (size_t)z1 * sstride);
             const float4 B = make_float4(fmaf(W.x, cz, d * M.x), fmaf(W.y, cz, d * M.y),
                                          fmaf(W.z, cz, d * M.z), fmaf(W.w, cz, d * M.w));
             const float4 A = make_float4(W.x - B.x, W.y - B.y, W.z - B.z, W.w - B.w);
@@ -986,7 +1017,7 @@ int zt_lg(const ct_plan *p) {
 // Work of the transpose: per-volume maxima, then (lanes-along-z path) the
 // pixel tables and the z-major copy of the volumes.
 struct ZtWork {
-    size_t vmax, px, py, span, vol_t, total;
+    size_t vmax, px, py, pxl, pyl, span, vol_t, total;
 };
 
 ZtWork zt_work(const ct_plan *p, int batch) {
@@ -1000,6 +1031,10 @@ ZtWork zt_work(const ct_plan *p, int batch) {
     w.px = o;
     o += align256(sizeof(float) * (size_t)p->g.nx);
     w.py = o;
+    o += align256(sizeof(float) * (size_t)p->g.ny);
+    w.pxl = o;
+    o += align256(sizeof(float) * (size_t)p->g.nx);
+    w.pyl = o;
     o += align256(sizeof(float) * (size_t)p->g.ny);
     w.span = o;
     o += align256(sizeof(int2) * (size_t)p->g.ny);
@@ -1051,15 +1086,19 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
     cudaError_t e0 = cudaMemsetAsync(vmax_bits, 0, sizeof(int) * (size_t)batch, s);
     if (e0 != cudaSuccess) return (int)e0;
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
+    const float2 *vcs_lo = reinterpret_cast<const float2 *>(p->d_view_cs_lo);
+    const float2 *col_tan = reinterpret_cast<const float2 *>(p->d_col_tan);
     const bool tex = p->opts.texture_weights != 0;
     const size_t per_volume = (size_t)a.nz * a.ny * a.nx;
     if (const size_t smem = zt_smem(p)) {
         const int npix = a.nx * a.ny, nzp = zt_nzp(p);
         float *px = reinterpret_cast<float *>(wb + zw.px);
         float *py = reinterpret_cast<float *>(wb + zw.py);
+        float *pxl = reinterpret_cast<float *>(wb + zw.pxl);
+        float *pyl = reinterpret_cast<float *>(wb + zw.pyl);
         int2 *span = reinterpret_cast<int2 *>(wb + zw.span);
         float *vol_t = reinterpret_cast<float *>(wb + zw.vol_t);
-        cone_fov_tables_kernel<<<a.ny, 32, 0, s>>>(a, px, py, span);
+        cone_fov_tables_kernel<<<a.ny, 32, 0, s>>>(a, px, py, pxl, pyl, span);
         ct_count_launch();
         auto kern = a.atan_deg == 4   ? (tex ? cone_bp_transpose_z_kernel<4, true>
                                              : cone_bp_transpose_z_kernel<4, false>)
@@ -1075,8 +1114,8 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
             cone_zmajor_kernel<<<dim3((npix + 31) / 32, (nzp + 31) / 32, nb), 256, 0, s>>>(
                 vol + (size_t)b0 * per_volume, vol_t, vmax_bits + b0, a.nz, npix, nzp);
             kern<<<dim3(a.V, nb), kZThreads, smem, s>>>(
-                vol_t, proj + (size_t)b0 * a.V * a.n_rows * a.C, vcs, p->d_view_z,
-                vmax_bits + b0, px, py, span, a, nzp, zt_lg(p));
+                vol_t, proj + (size_t)b0 * a.V * a.n_rows * a.C, vcs, vcs_lo, col_tan,
+                p->d_view_z, vmax_bits + b0, px, py, pxl, pyl, span, a, nzp, zt_lg(p));
             ct_count_launch(2);
         }
         return (int)cudaGetLastError();
@@ -1098,7 +1137,7 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
         const int nb = batch - b0 < per ? batch - b0 : per;
         kern<<<dim3(a.V, rblocks * nb), kThreads, smem, (cudaStream_t)stream>>>(
             vol + (size_t)b0 * a.nz * a.ny * a.nx, proj + (size_t)b0 * a.V * a.n_rows * a.C, vcs,
-            p->d_view_z, vmax_bits + b0, a, nb);
+            vcs_lo, col_tan, p->d_view_z, vmax_bits + b0, a, nb);
         ct_count_launch();
     }
     return (int)cudaGetLastError();

@@ -222,9 +222,10 @@ __global__ void __launch_bounds__(kGThreads, adj_min_blocks(SB))
                 const float W11 = P, W10 = F - P, W01 = G - P, W00 = cnt - F - G + P;
                 const unsigned long long p00 = pack2(W00, W00), p10 = pack2(W10, W10);
                 const unsigned long long p01 = pack2(W01, W01), p11 = pack2(W11, W11);
+                const bool ok = (unsigned)c < (unsigned)a.C;
 #pragma unroll
                 for (int q = 0; q < SB / 4; ++q) {
-                    const float4 val = __ldg(sb + (row + c) * (SB / 4) + q);
+                    const float4 val = CT_DLOAD(ok, sb + (row + c) * (SB / 4) + q);
                     const unsigned long long lo = pack2(val.x, val.y), hi = pack2(val.z, val.w);
                     w00[2 * q] = fma2(p00, lo, w00[2 * q]);
                     w00[2 * q + 1] = fma2(p00, hi, w00[2 * q + 1]);

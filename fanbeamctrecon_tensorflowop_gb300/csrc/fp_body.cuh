@@ -47,11 +47,13 @@ struct Taps {
     unsigned long long acc[SB];
     __device__ __forceinline__ void add(const CellWeights &cw, int cu, int cv) {
         const int qi = min(max(cu + 1, 0), Q - 1), qj = min(max(cv + 1, 0), Q - 1);
+        // the walk stays on cells -1 .. nx-1 (quads 0 .. nx): the clamp is a guard
+        const bool ok = (unsigned)(cu + 1) < (unsigned)Q && (unsigned)(cv + 1) < (unsigned)Q;
         const float4 *p = q + (size_t)qj * Q + qi;
         const unsigned long long wa = pack2(cw.w00, cw.w10), wb = pack2(cw.w01, cw.w11);
 #pragma unroll
         for (int s = 0; s < SB; ++s) {
-            const float4 t = __ldg(p + s * stride);
+            const float4 t = CT_DLOAD(ok, p + s * stride);
             acc[s] = fma2(wa, pack2(t.x, t.y), acc[s]);
             acc[s] = fma2(wb, pack2(t.z, t.w), acc[s]);
         }

@@ -86,10 +86,25 @@ ct_status ct_validate_geom(const ct_fan_geom *g) {
 void ct_build_view_table(const ct_fan_geom *g, const float *angles, ct_host_tables *t) {
     const int V = g->n_views;
     t->view_cs.assign(2 * (size_t)V, 0.0f);
+    t->view_cs_lo.assign(2 * (size_t)V, 0.0f);
     for (int v = 0; v < V; ++v) {
         const double beta = angles[v];
-        t->view_cs[2 * v + 0] = static_cast<float>(-std::cos(beta));
-        t->view_cs[2 * v + 1] = static_cast<float>(-std::sin(beta));
+        const double c = -std::cos(beta), s = -std::sin(beta);
+        t->view_cs[2 * v + 0] = static_cast<float>(c);
+        t->view_cs[2 * v + 1] = static_cast<float>(s);
+        t->view_cs_lo[2 * v + 0] = static_cast<float>(c - (double)t->view_cs[2 * v + 0]);
+        t->view_cs_lo[2 * v + 1] = static_cast<float>(s - (double)t->view_cs[2 * v + 1]);
+    }
+    // column boundaries y = b: gamma_b = left + (b - shift - 1/2) dcol, the
+    // inverse of y = (gamma - left)/dcol + shift + 1/2 (BP/transform.cu:86)
+    const int C = g->n_cols;
+    t->col_tan.assign(2 * (size_t)(C + 1), 0.0f);
+    for (int b = 0; b <= C; ++b) {
+        const double tg =
+            std::tan((double)g->left + ((double)b - (double)g->shift - 0.5) * (double)g->dcol);
+        const float hi = static_cast<float>(tg);
+        t->col_tan[2 * (size_t)b] = hi;
+        t->col_tan[2 * (size_t)b + 1] = static_cast<float>(tg - (double)hi);
     }
 }
 

@@ -19,6 +19,10 @@ struct ct_host_tables {
     // Per view: rotation constants as the reference BP kernels take them,
     // c = -cos(beta), s = -sin(beta) (BP/transform.cu:116).
     std::vector<float> view_cs;      // [2*V]
+    // the rounding left by view_cs: (-cos(beta) - c, -sin(beta) - s) (float-float pairs)
+    std::vector<float> view_cs_lo;   // [2*V]
+    // per column boundary y = b (b = 0..C): tan(left + (b - shift - 1/2) dcol) as hi, lo
+    std::vector<float> col_tan;      // [2*(C+1)]
     // Per ray (view-major, [V][C]): start (x, y) and step (x, y) in texture
     // pixel coordinates, and the sample count floor(chord/0.125)
     // (FP/transform.cu:64-101).
@@ -85,6 +89,8 @@ struct ct_plan {
     std::vector<float> h_view_cs;    // host copy of the view table
     // device copies of ct_host_tables (owned)
     float *d_view_cs;                // [2V]
+    float *d_view_cs_lo;             // [2V] float-float remainder of d_view_cs
+    float *d_col_tan;                // [2(C+1)] tan of the column boundaries (hi, lo)
     float *d_ray;                    // [4VC]
     float *d_ray_inv;                // [2VC] 1/step (1e30 for a zero step), adjoint gather
     int32_t *d_nsamp;                // [VC]

@@ -48,7 +48,8 @@ typedef enum ct_status {
     CT_ERR_CUDA = 4,             /* a CUDA runtime call or launch failed */
     CT_ERR_ALLOC = 5,            /* device or host allocation failed */
     CT_ERR_UNSUPPORTED = 6,      /* valid request this build cannot run */
-    CT_ERR_TIMEOUT = 7           /* a bounded device-side wait gave up */
+    CT_ERR_TIMEOUT = 7,          /* a bounded device-side wait gave up */
+    CT_ERR_DEVICE_CHECK = 8      /* debug builds: a kernel's index check failed */
 } ct_status;
 
 /* Fan-beam geometry decoded from the reference's 16-float `parameter`
@@ -157,6 +158,16 @@ const char *ct_last_error(void);
 /* Number of kernels this library has launched in this process. */
 uint64_t ct_launch_count(void);
 
+/* Build flags: CT_BUILD_INDEX_CHECKS is set in debug builds (compiled with
+ * -DCT_DEBUG), whose kernels test every gather index against the array it
+ * reads, skip an access outside it (reading zero) and record where; the next
+ * ct_plan_check then returns CT_ERR_DEVICE_CHECK (ct_last_error names the
+ * source line).  Release builds carry no checks and return 0.  No counterpart
+ * in the reference (its kernels checked no index; checkCudaErrors exited the
+ * process on any CUDA error, FP/transform.cu:4). */
+#define CT_BUILD_INDEX_CHECKS 1u
+uint32_t ct_build_flags(void);
+
 /* ---- device memory ----------------------------------------------------------- */
 
 /* A caller-supplied device allocator.  The library takes device memory in
@@ -219,7 +230,10 @@ ct_status ct_plan_create(const ct_fan_geom *geom, const float *angles, int n_ang
 ct_status ct_plan_destroy(ct_plan *plan);
 /* Waits for the device and reports CT_ERR_TIMEOUT (and clears the flag) if
  * a kernel of this plan hit the iteration limit of one of its bounded waits
- * since the last check (only the tensor-core filter waits on barriers). */
+ * since the last check (only the tensor-core filter waits on barriers).  In
+ * debug builds (ct_build_flags) it then reports CT_ERR_DEVICE_CHECK (and
+ * clears the flags) if any kernel of the library failed an index check since
+ * the last call; those flags are per device, not per plan. */
 ct_status ct_plan_check(const ct_plan *plan);
 /* Failure-path self-test: enqueues one thread that waits, with the filter's
  * bounded-wait code, on a barrier nothing completes, gives up after budget_us
