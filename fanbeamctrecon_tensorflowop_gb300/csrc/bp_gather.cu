@@ -48,9 +48,16 @@ struct BptArgs {
 
 __device__ __forceinline__ unsigned long long dup2(float x) { return pack2(x, x); }
 
+#ifndef CT_BPG_MINB
+#define CT_BPG_MINB 1
+#endif
+#ifndef CT_BPG_NQ
+#define CT_BPG_NQ 4
+#endif
+
 // NQ quads = 4 NQ slices per launch slice group (blockIdx.y).
 template <bool WEIGHTED, int NQ>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, CT_BPG_MINB)
     bp_gather_kernel(const float4 *__restrict__ rows, const float4 *__restrict__ cols,
                      size_t qplane, float *__restrict__ sino, int nsl,
                      const int4 *__restrict__ wtab, const longlong2 *__restrict__ btab,
@@ -105,13 +112,13 @@ __global__ void __launch_bounds__(128)
                 const float dp = (float)(i - hl) - F;  // offset from the lower boundary (pixels)
                 const float n = dp * rr.z;              // normal distance (mm)
                 const float L = fmaf(dp, rr.w, Lb);     // distance along the boundary ray (mm)
-                const float q = n * __frcp_rn(L);
+                const float q = __fdividef(n, L);
                 const float q2 = q * q;
                 // atan(q) for |q| <= dcol: q (1 - q^2/3 + q^4/5)
                 const float f = q * fmaf(q2, fmaf(q2, 0.2f, -0.33333334f), 1.0f) * a.inv_dcol;
                 float wa = 1.0f - f, wb = f;
                 if (WEIGHTED) {
-                    const float w = __frcp_rn(fmaf(L, L, n * n));  // 1 / (U^2 + t^2)
+                    const float w = __fdividef(1.0f, fmaf(L, L, n * n));  // 1 / (U^2 + t^2)
                     wa *= w;
                     wb *= w;
                 }
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(256)
 
 constexpr int kChunk = 64;  // slices per pass (quad planes of 16 slice quads)
 
-int quads_per_group(int nb) { return nb <= 4 ? 1 : (nb <= 8 ? 2 : 4); }
+int quads_per_group(int nb) { return nb <= 4 ? 1 : (nb <= 8 || CT_BPG_NQ < 4 ? 2 : 4); }
 
 int padded_quads(int nb) {
     const int nq = quads_per_group(nb);

@@ -1058,15 +1058,29 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
                       void *stream) {
     ConeArgs a = make_cone_args(p);
     {
-        // in pixels of the smaller pitch and in slices; mm otherwise
+        // Bounds of a detector cell's weighted sample counts (rigorous; the
+        // fixed-point scale is 2^30 over their product with max|vol| and max w).
+        // Columns: a cell's pixels carry the column hat weight (unit integral,
+        // support two channels).  Layer by layer the hat's level sets are
+        // wedges from the source cut by the FOV disc, convex, and a convex set
+        // holds at most area/(dx dy) + perimeter/(2 min(dx, dy)) + 1 lattice
+        // points (Nosarzewska); summed over the layers, the area term is
+        // dcol (L2^2 - L1^2)/2 <= dcol 2 R rf and the perimeter term at most
+        // (4 rf + 2 pi dcol (R + rf))/2.  The same holds for the clamped edge
+        // channels, whose weight is a trapezoid of the same integral.  Rows:
+        // a pixel's slices sample the row coordinate at a step of at least
+        // dz D / ((R + rf) drow), so a row's hat weights sum to at most
+        // 1/step + 1 (a unimodal function's Riemann sum exceeds its integral by
+        // at most its maximum).  (2-channel and 2-row counts, 4.8x and 2x
+        // looser at the clinical geometry, quantised the FDK adjoint into a
+        // 1.5e-4 error after its ramp filter.)
         const double pix = p->g.dx < p->g.dy ? p->g.dx : p->g.dy;
         const double R = p->g.sid, rf = p->g.rfov, D = p->g.sdd;
-        // pixel centres within two channels of a column: a wedge 2 dcol L wide
-        const double width = 2.0 * (double)p->g.dcol * (R + rf) / pix + 2.0;
-        const double length = 2.0 * rf / pix + 2.0;
-        a.fix_npix = (float)(width * length);
-        // slice centres within one row (drow L / D at the detector) either side
-        a.fix_slices = (float)(2.0 * (double)p->g.drow * (R + rf) / (D * (double)p->g.dz) + 2.0);
+        const double dcol = p->g.dcol;
+        a.fix_npix = (float)(dcol * 2.0 * R * rf / ((double)p->g.dx * (double)p->g.dy) +
+                             (2.0 * rf + 3.14159265358979 * dcol * (R + rf)) / pix + 1.0);
+        const double rstep = (double)p->g.dz * D / ((R + rf) * (double)p->g.drow);
+        a.fix_slices = (float)(1.0 / rstep + 1.0);
         a.fix_wmax = (float)(1.0 / ((R - rf) * (R - rf)));
         // row + 1/2 = z row_scale / U + row_off over the slice centres
         // relative to every source height and U in [R - rf, R + rf]; no

@@ -104,4 +104,6 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {Path(__file__).name} <reference checkout>")
+    main(Path(sys.argv[1]))
