@@ -48,9 +48,13 @@ struct BptArgs {
 
 __device__ __forceinline__ unsigned long long dup2(float x) { return pack2(x, x); }
 
+// 5 resident blocks per SM (96 registers): 32 clinical slices, BP / FBP
+// adjoint 2.70 / 3.34 ms, against 3.71 / 4.25 ms at the compiler's 102
+// registers (4 blocks) and 3.42 / 3.99 ms at 6 blocks (80 registers)
 #ifndef CT_BPG_MINB
-#define CT_BPG_MINB 1
+#define CT_BPG_MINB 5
 #endif
+// at most NQ slice quads per lane (16 slices); 8 slices measured 5.18 ms
 #ifndef CT_BPG_NQ
 #define CT_BPG_NQ 4
 #endif

@@ -51,6 +51,32 @@ __device__ __forceinline__ void ff_ut(float xh, float xl, float yh, float yl, fl
     U.l = us.l + s12.l + f1 + f2 + fmaf(xh, cl, fmaf(xl, ch, fmaf(yh, sl, yl * sh)));
 }
 
+// The row part of ff_ut for an image row at y: t_row = y c, U_row = R + y s.
+__device__ __forceinline__ void ff_row(float yh, float yl, float ch, float cl, float sh,
+                                       float sl, float R, FF &t_row, FF &U_row) {
+    const float a = yh * ch;
+    t_row.h = a;
+    t_row.l = fmaf(yh, ch, -a) + fmaf(yh, cl, yl * ch);
+    const float b = yh * sh;
+    const FF us = ff_two_sum(R, b);
+    U_row.h = us.h;
+    U_row.l = us.l + fmaf(yh, sh, -b) + fmaf(yh, sl, yl * sh);
+}
+
+// Completes ff_row for the pixel at x: t = t_row - x s, U = U_row + x c.
+__device__ __forceinline__ void ff_pixel(float xh, float xl, float ch, float cl, float sh,
+                                         float sl, const FF &t_row, const FF &U_row, FF &U,
+                                         FF &t) {
+    const float p = -xh * sh;
+    const FF ts = ff_two_sum(t_row.h, p);
+    t.h = ts.h;
+    t.l = ts.l + fmaf(-xh, sh, -p) + t_row.l + fmaf(-xh, sl, -xl * sh);
+    const float q = xh * ch;
+    const FF us = ff_two_sum(U_row.h, q);
+    U.h = us.h;
+    U.l = us.l + fmaf(xh, ch, -q) + U_row.l + fmaf(xh, cl, xl * ch);
+}
+
 // Strip ic (from the FP32 column coordinate) and the precise fraction f of
 // the pixel's angle from the strip's lower boundary, in channels; ic and f
 // are corrected when the FP32 strip was one off.  tan_b: [C+1] (hi, lo) of

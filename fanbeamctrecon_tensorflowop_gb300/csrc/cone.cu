@@ -388,7 +388,11 @@ __global__ void __launch_bounds__(256)
 #define CT_CONE_ZT_THREADS 1024
 #endif
 constexpr int kZThreads = CT_CONE_ZT_THREADS;
-constexpr int kZS = 8;  // consecutive slices per lane
+#ifndef CT_CONE_ZS
+#define CT_CONE_ZS 8
+#endif
+constexpr int kZS = CT_CONE_ZS;  // consecutive slices per lane (8 or 16)
+constexpr int kZQ = kZS / 4;     // their float4 loads
 
 // [B][nz][ny*nx] -> [B][ny*nx][nzp] (nzp = nz rounded up to kZS, zero-filled),
 // and per volume max |vol| into vmax_bits (which must start at zero).
@@ -527,27 +531,37 @@ __global__ void __launch_bounds__(kZThreads, 1)
     const int G = nzp / kZS;                 // slice groups per pixel
     const float *vb = vol_t + (size_t)b * a.nx * a.ny * nzp;
     const float4 zero4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    auto load = [&](const ZtCursor &c, float4 &x0, float4 &x1) {
+    auto load = [&](const ZtCursor &c, float4 *x) {
         const int ix = c.x0 + c.t * per + slot;
-        x0 = x1 = zero4;
+#pragma unroll
+        for (int q = 0; q < kZQ; ++q) x[q] = zero4;
         if (ix < c.end && g < G) {
-            const float4 *q = reinterpret_cast<const float4 *>(
+            const float4 *q4 = reinterpret_cast<const float4 *>(
                 vb + ((size_t)c.iy * a.nx + ix) * nzp + g * kZS);
-            x0 = __ldg(q);
-            x1 = __ldg(q + 1);
+#pragma unroll
+            for (int q = 0; q < kZQ; ++q) x[q] = __ldg(q4 + q);
         }
     };
     ZtCursor cur{-1, 0, 0, 0, 0};
     bool have = cur.next(span, a.ny, warp, NW, per);
-    float4 va = zero4, vc = zero4;  // this lane's 8 slices of the current pixel
-    if (have) load(cur, va, vc);
+    float4 va[kZQ];  // this lane's kZS slices of the current pixel
+    if (have) load(cur, va);
+    // float-float t and U of the current image row's y (warp-uniform row):
+    // t = y c - x s, U = R + y s + x c, completed per pixel (colprec.cuh)
+    int frow = -1;
+    FF trow{0.0f, 0.0f}, urow{0.0f, 0.0f};
     while (have) {
         // the next tile's loads go out before this tile's work
         ZtCursor nxt = cur;
         const bool more = nxt.next(span, a.ny, warp, NW, per);
-        float4 na = zero4, nc = zero4;
-        if (more) load(nxt, na, nc);
+        float4 na[kZQ];
+        if (more) load(nxt, na);
         const int ix = cur.x0 + cur.t * per + slot;
+        if (!TEX && cur.iy != frow) {
+            const float yh = __ldg(py_tab + cur.iy), yl = __ldg(pyl_tab + cur.iy);
+            ff_row(yh, yl, cs.x, csl.x, cs.y, csl.y, a.R, trow, urow);
+            frow = cur.iy;
+        }
         if (ix < cur.end && g < G) {
             const float px = __ldg(px_tab + ix), py = __ldg(py_tab + cur.iy);
             const float U = fmaf(px, cs.x, fmaf(py, cs.y, a.R));
@@ -561,8 +575,8 @@ __global__ void __launch_bounds__(kZThreads, 1)
                 const float A = floorf(fmaf(f, 256.0f, 0.5f));  // used with TEX only
                 if constexpr (!TEX) {  // the column fraction from float-float geometry
                     FF Uf, tf;
-                    ff_ut(px, __ldg(pxl_tab + ix), py, __ldg(pyl_tab + cur.iy), cs.x, csl.x, cs.y,
-                          csl.y, a.R, Uf, tf);
+                    ff_pixel(px, __ldg(pxl_tab + ix), cs.x, csl.x, cs.y, csl.y, trow, urow, Uf,
+                             tf);
                     precise_strip(Uf, tf, col_tan, a.inv_dcol, a.C, ic, f);
                 }
                 int *c0 = acc + max(ic - 1, 0) * ld;
@@ -583,14 +597,19 @@ __global__ void __launch_bounds__(kZThreads, 1)
                 for (int kb = g * kZS; kb < a.nz; kb += gp * kZS) {
                     float x[kZS];
                     if (kb == g * kZS) {
-                        x[0] = va.x, x[1] = va.y, x[2] = va.z, x[3] = va.w;
-                        x[4] = vc.x, x[5] = vc.y, x[6] = vc.z, x[7] = vc.w;
+#pragma unroll
+                        for (int q = 0; q < kZQ; ++q)
+                            x[4 * q] = va[q].x, x[4 * q + 1] = va[q].y, x[4 * q + 2] = va[q].z,
+                                   x[4 * q + 3] = va[q].w;
                     } else {
-                        const float4 *q = reinterpret_cast<const float4 *>(
+                        const float4 *q4 = reinterpret_cast<const float4 *>(
                             vb + ((size_t)cur.iy * a.nx + ix) * nzp + kb);
-                        const float4 u0 = __ldg(q), u1 = __ldg(q + 1);
-                        x[0] = u0.x, x[1] = u0.y, x[2] = u0.z, x[3] = u0.w;
-                        x[4] = u1.x, x[5] = u1.y, x[6] = u1.z, x[7] = u1.w;
+#pragma unroll
+                        for (int q = 0; q < kZQ; ++q) {
+                            const float4 u = __ldg(q4 + q);
+                            x[4 * q] = u.x, x[4 * q + 1] = u.y, x[4 * q + 2] = u.z,
+                                   x[4 * q + 3] = u.w;
+                        }
                     }
                     // the lane's slices lie in one group of kZC (kZS divides kZC)
                     const int kg = kb & ~(kZC - 1);
@@ -636,8 +655,8 @@ __global__ void __launch_bounds__(kZThreads, 1)
                 }
             }
         }
-        va = na;
-        vc = nc;
+#pragma unroll
+        for (int q = 0; q < kZQ; ++q) va[q] = na[q];
         cur = nxt;
         have = more;
     }

@@ -14,8 +14,6 @@
 // (128-byte swizzle), splits the input tile, and one thread issues 4 K-slices
 // x 3 tcgen05.mma (M=128, N=224, K=8, kind::tf32) into a 128 x 256-column
 // TMEM accumulator; four warps then read the accumulator with tcgen05.ld.
-// K steps run through a two-stage shared-memory pipeline (loads and split of
-// step kt+1 overlap the MMAs of step kt).
 // All mbarrier waits are bounded: on a timeout the CTA raises the plan's
 // error flag, releases its tensor memory and exits.
 #include <cuda.h>
@@ -40,11 +38,7 @@ constexpr int TC_TMEM_COLS = 256;   // power of two >= TC_BN
 constexpr int TC_THREADS = 128;
 constexpr unsigned TC_A_BYTES = TC_BM * TC_BK * 4;  // 16 KB
 constexpr unsigned TC_B_BYTES = TC_BN * TC_BK * 4;  // 28 KB
-// one pipeline stage: the input tile (split in place: it becomes the low
-// part), its high part, and the two tap tiles
-constexpr unsigned TC_STAGE = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 88 KB
-constexpr int TC_STAGES = 2;
-constexpr unsigned TC_SMEM = 1024 /*align slack*/ + TC_STAGES * TC_STAGE + 64;
+constexpr unsigned TC_SMEM = 1024 /*align slack*/ + 3 * TC_A_BYTES + 2 * TC_B_BYTES + 64;
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
                                             uint64_t *bar) {
@@ -95,11 +89,6 @@ __device__ __forceinline__ float tf32_hi(float x) {
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
-// Two-stage pipeline: while the tensor core multiplies K step kt from one
-// stage, the copies of step kt+1 land in the other and the threads split
-// them (the split of kt+1 waits only for the MMAs of kt-1, which read that
-// stage).  Barriers: full[s] completes when stage s's copies land, empty[s]
-// when the MMAs that read stage s are done (tcgen05.commit).
 __global__ void __launch_bounds__(TC_THREADS)
     ramp_tc_kernel(const __grid_constant__ CUtensorMap map_in,
                    const __grid_constant__ CUtensorMap map_bhi,
@@ -109,29 +98,22 @@ __global__ void __launch_bounds__(TC_THREADS)
     // 1024-byte aligned buffers (the 128-byte swizzle atom)
     uint8_t *base = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    // stage st: input (then its low part), its high part, tap tiles hi and lo
-    auto sA = [&](int st) { return reinterpret_cast<float *>(base + st * TC_STAGE); };
-    auto sAhi = [&](int st) { return reinterpret_cast<float *>(base + st * TC_STAGE + TC_A_BYTES); };
-    auto sBhi = [&](int st) {
-        return reinterpret_cast<float *>(base + st * TC_STAGE + 2 * TC_A_BYTES);
-    };
-    auto sBlo = [&](int st) {
-        return reinterpret_cast<float *>(base + st * TC_STAGE + 2 * TC_A_BYTES + TC_B_BYTES);
-    };
-    uint64_t *bars = reinterpret_cast<uint64_t *>(base + TC_STAGES * TC_STAGE);
-    uint64_t *full_bar = bars, *empty_bar = bars + TC_STAGES;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TC_STAGES);
+    float *sA = reinterpret_cast<float *>(base);
+    float *sAhi = reinterpret_cast<float *>(base + TC_A_BYTES);
+    float *sAlo = reinterpret_cast<float *>(base + 2 * TC_A_BYTES);
+    float *sBhi = reinterpret_cast<float *>(base + 3 * TC_A_BYTES);
+    float *sBlo = reinterpret_cast<float *>(base + 3 * TC_A_BYTES + TC_B_BYTES);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + 3 * TC_A_BYTES + 2 * TC_B_BYTES);
+    uint64_t *full_bar = bars, *mma_bar = bars + 1;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m0 = blockIdx.x * TC_BM;
     const int n0 = blockIdx.y * TC_BN;
 
     if (tid == 0) {
-#pragma unroll
-        for (int st = 0; st < TC_STAGES; ++st) {
-            mbar_init(full_bar + st, 1);
-            mbar_init(empty_bar + st, 1);
-        }
+        mbar_init(full_bar, 1);
+        mbar_init(mma_bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -147,27 +129,21 @@ __global__ void __launch_bounds__(TC_THREADS)
     const uint32_t tmem = *tmem_slot;
     const uint32_t idesc = tf32_idesc(TC_BM, TC_BN);
 
-    int last_issued = 0;  // (thread 0) the last K step whose copies were issued
-    auto issue_loads = [&](int kt) {
-        const int st = kt & 1;
-        last_issued = kt;
-        mbar_expect_tx(full_bar + st, TC_A_BYTES + 2 * TC_B_BYTES);
-        tma_load_2d(sA(st), &map_in, kt * TC_BK, m0, full_bar + st);
-        tma_load_2d(sBhi(st), &map_bhi, kt * TC_BK, n0, full_bar + st);
-        tma_load_2d(sBlo(st), &map_blo, kt * TC_BK, n0, full_bar + st);
-    };
-    if (tid == 0) issue_loads(0);
-
     bool ok = true;
     for (int kt = 0; kt < k_tiles && ok; ++kt) {
-        const int st = kt & 1;
-        ok = mbar_wait(full_bar + st, (kt >> 1) & 1);
-        // split the input tile: high part to sAhi, low part in place (the
-        // layout, swizzle included, is elementwise the same)
+        const uint32_t phase = kt & 1;
+        if (tid == 0) {
+            mbar_expect_tx(full_bar, TC_A_BYTES + 2 * TC_B_BYTES);
+            tma_load_2d(sA, &map_in, kt * TC_BK, m0, full_bar);
+            tma_load_2d(sBhi, &map_bhi, kt * TC_BK, n0, full_bar);
+            tma_load_2d(sBlo, &map_blo, kt * TC_BK, n0, full_bar);
+        }
+        ok = mbar_wait(full_bar, phase);
+        // split the input tile in place of layout (elementwise, swizzle kept)
         if (ok) {
-            float4 *src = reinterpret_cast<float4 *>(sA(st));
-            float4 *dhi = reinterpret_cast<float4 *>(sAhi(st));
-#pragma unroll 4
+            const float4 *src = reinterpret_cast<const float4 *>(sA);
+            float4 *dhi = reinterpret_cast<float4 *>(sAhi);
+            float4 *dlo = reinterpret_cast<float4 *>(sAlo);
             for (int q = tid; q < (int)(TC_A_BYTES / 16); q += TC_THREADS) {
                 const float4 x = src[q];
                 float4 h, l;
@@ -176,16 +152,17 @@ __global__ void __launch_bounds__(TC_THREADS)
                 h.z = tf32_hi(x.z); l.z = x.z - h.z;
                 h.w = tf32_hi(x.w); l.w = x.w - h.w;
                 dhi[q] = h;
-                src[q] = l;
+                dlo[q] = l;
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
         ok = __syncthreads_and(ok);
         if (!ok) break;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t ahi = smem_u32(sAhi(st)), alo = smem_u32(sA(st));
-            const uint32_t bhi = smem_u32(sBhi(st)), blo = smem_u32(sBlo(st));
+            const uint32_t ahi = smem_u32(sAhi), alo = smem_u32(sAlo);
+            const uint32_t bhi = smem_u32(sBhi), blo = smem_u32(sBlo);
 #pragma unroll
             for (int s = 0; s < TC_BK / 8; ++s) {
                 const uint32_t off = s * 32;  // 8 TF32 = 32 bytes along K
@@ -194,23 +171,12 @@ __global__ void __launch_bounds__(TC_THREADS)
                 mma_tf32(tmem, sw128_desc(ahi + off), sw128_desc(blo + off), idesc, 1u);
                 mma_tf32(tmem, sw128_desc(alo + off), sw128_desc(bhi + off), idesc, 1u);
             }
-            mma_commit(empty_bar + st);
-            // the next step's copies go to the other stage once the MMAs of
-            // step kt-1, which read it, are done
-            if (kt + 1 < k_tiles) {
-                bool free_ok = true;
-                if (kt >= 1) free_ok = mbar_wait(empty_bar + (st ^ 1), ((kt - 1) >> 1) & 1);
-                if (free_ok)
-                    issue_loads(kt + 1);
-                else
-                    ok = false;
-            }
+            mma_commit(mma_bar);
         }
+        // the MMAs must finish reading shared memory before the next loads
+        ok = mbar_wait(mma_bar, phase);
         ok = __syncthreads_and(ok);
     }
-    // all MMAs done before the accumulator is read
-    if (ok && k_tiles > 0) ok = mbar_wait(empty_bar + ((k_tiles - 1) & 1), ((k_tiles - 1) >> 1) & 1);
-    ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok) {
         // epilogue: warp w reads accumulator lanes 32w..32w+31 (rows m0+32w+lane)
@@ -241,10 +207,6 @@ __global__ void __launch_bounds__(TC_THREADS)
     } else if (tid == 0) {
         atomicExch(err, 1);
     }
-    // after a wait gave up, the last copies issued may still be in flight:
-    // let them land (bounded as well) before the shared memory is released
-    if (!ok && tid == 0)
-        mbar_wait(full_bar + (last_issued & 1), (last_issued >> 1) & 1, 20000000ull);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
