@@ -660,6 +660,17 @@ def main() -> None:
     total_fbp, _, _ = timed(fbp_step, max(5, args.steps // 3), args.warmup)
     fbp_ms_per_slice = 1e3 * total_fbp / max(5, args.steps // 3) / BATCH
 
+    # ---- the Shepp-Logan ramp filter alone (tensor-core Toeplitz GEMM), 32 slices --------
+    fbuf = torch.empty_like(sinos[0])
+
+    def filter_step(k):
+        plan_sl.ramp_filter(sinos[k % POOL], out=fbuf)
+
+    n_f = max(5, args.steps // 3)
+    total_filt, _, _ = timed(filter_step, n_f, args.warmup)
+    filter_ms = 1e3 * total_filt / n_f
+    filter_tflops = 2.0 * BATCH * VIEWS * COLS * COLS / (total_filt / n_f) / 1e12
+
     # ---- batch-32 differentiable step: FP, residual, adjoint ------------------------
     target = [plan.fp(imgs[(k + 1) % POOL]) for k in range(2)]
     grads = [torch.empty((BATCH, N_PIX, N_PIX), device=dev) for _ in range(2)]
@@ -891,6 +902,8 @@ def main() -> None:
                 "bp_gpix_views_per_s": bp_gpv,
                 "bp_roofline": bp_roof,
                 "fbp_shepp_logan_ms_per_slice": fbp_ms_per_slice,
+                "filter_ms_batch32": filter_ms,
+                "filter_algorithmic_tflops": filter_tflops,
                 "batch32_fp_adjoint_ms": fa_ms,
                 "batch32_adjoint_only_ms": adj_ms,
                 "fp_adjoint_roofline": adj_roof,
