@@ -734,7 +734,7 @@ __global__ void __launch_bounds__(kZThreads, 1)
 constexpr int kConeSteps = 64;
 
 struct ConeFpArgs {
-    int V, C, nx, nz, n_rows, wpv;
+    int V, C, nx, ny, nz, n_rows, wpv;
     float w;        // 0.125*dx
     float D, det_bottom, drow, dz, zmin;
     int max_iter;
@@ -988,6 +988,365 @@ __global__ void __launch_bounds__(256)
                qi, qj);
 }
 
+// ---- cone-beam forward projection, one in-plane walk per ray for all rows ---------
+// The projector above walks a ray's in-plane cells once per group of RB
+// detector rows, and its lanes idle where neighbouring rays cut segments at
+// different z crossings.  This one gives a warp G adjacent channels of one
+// view and walks each ray's in-plane cells once for every row:
+//  - walk: lane L takes cell line m of ray L mod G along the ray's major axis
+//    (32/G lines of each ray per chunk), splits the line's samples at its one
+//    minor-axis boundary (a line holds at most two cells) and queues, per
+//    cell segment, its cell, first sample k, count and entry fractions and
+//    the moments W_c = sum_j q_c(j), M_c = sum_j j q_c(j) of the bilinear
+//    weights, in shared memory;
+//  - drain: for every queued segment all lanes take the detector rows (lane
+//    l: rows l, l+32, ...) and add W.t0 + cz W.(t1 - t0) + dw M.(t1 - t0) with
+//    t0, t1 the four bilinear taps of slices kz, kz+1, cz the row's z
+//    fraction at sample k and dw its z step per sample.  The taps come from
+//    z-major columns of x pairs (two 8-byte loads per slice, each landing as
+//    an f32x2 operand); rows read consecutive slices, so one warp load covers
+//    a few lines.  The dw M.(t1 - t0) term is summed per row and scaled by dw
+//    at the end;
+//  - crossings: that sum is the linear extension, from the segment's first
+//    sample, of the clamped piecewise-linear z interpolant.  Past each slice
+//    boundary b that a row crosses inside the segment the interpolant differs
+//    from it by sign(dw) (w - b) D2_b, D2_b the second difference of the
+//    quads about b.  The drain marks those (segment, row) pairs in per-lane
+//    bit masks, and after the chunk the lanes add the corrections together
+//    from the partial moments over the samples past b.
+// Columns hold slices -1 .. nz (slices -1 and nz repeat 0 and nz-1, so the
+// clamped interpolant needs no index clamp: z positions clamp to [-1, nz-1]),
+// nzp = nz + 2 entries per column.
+constexpr int kSegPerLane = 3;  // cell segments of one line (two, plus a rounding spare)
+constexpr int kSegSlots = 32 * kSegPerLane;
+
+struct SegQueue {
+    float4 e[kSegSlots];   // (column offset bits, second column offset bits, first sample k,
+                           //  count - 1)
+    float4 W[kSegSlots];   // sum_j q_c(j)
+    float4 M[kSegSlots];   // sum_j j q_c(j)
+    float2 f[kSegSlots];   // entry fractions (u, v)
+    float4 ray;            // the warp's ray: entry point and steps (read per chunk, which
+                           // keeps the walk's state out of the drain's registers)
+};
+
+// Launch shape (one clinical volume, CUDA events): 4-warp blocks, 7 resident
+// per SM (72 registers) 36.8 ms; 6 / 5 per SM 39.0 / 41.7 ms, 8 per SM (spills)
+// 40.1 ms.  z-major float4 quad columns instead of x pairs: 36.6 ms at twice
+// the workspace; view-major block order or tiles of 4 .. 64 views instead of
+// channel-group-major: 41 .. 51 ms.
+#ifndef CT_CONE_SEG_WARPS
+#define CT_CONE_SEG_WARPS 4
+#endif
+#ifndef CT_CONE_SEG_MINB
+#define CT_CONE_SEG_MINB 7
+#endif
+
+// x-pair columns: for image row y and xq in [0, nx] the pairs
+// (v(xq-1, y, z), v(xq, y, z)) of slices z = -1 .. nz (x and z clamped), nzp
+// float2 per column; a cell (cu, cv) reads the columns (cu+1, cv) and
+// (cu+1, cv+1), y clamped.
+__global__ void __launch_bounds__(256)
+    cone_pairs_z_kernel(const float *__restrict__ vol, float2 *__restrict__ pz, int nx, int ny,
+                        int nz, int nzp) {
+    __shared__ float2 tile[32][33];
+    const int X = nx + 1;
+    const int xq0 = blockIdx.x * 32, y = blockIdx.y, z0 = blockIdx.z * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int zz = ty; zz < 32; zz += 8) {
+        const int zp = z0 + zz, xq = xq0 + tx;
+        if (xq < X && zp < nzp) {
+            const float *sl = vol + (size_t)min(max(zp - 1, 0), nz - 1) * nx * ny + (size_t)y * nx;
+            tile[tx][zz] = make_float2(__ldg(sl + max(xq - 1, 0)), __ldg(sl + min(xq, nx - 1)));
+        }
+    }
+    __syncthreads();
+    for (int ii = ty; ii < 32; ii += 8) {
+        const int zp = z0 + tx;
+        if (xq0 + ii < X && zp < nzp) pz[((size_t)y * X + xq0 + ii) * nzp + zp] = tile[ii][tx];
+    }
+}
+
+// The correction of one (segment, row) pair for the slice boundaries the row
+// crosses inside the segment (see above); col points at slice 0 of the cell's
+// column.
+template <class Taps>
+__device__ __forceinline__ float cone_seg_crossings(Taps tap, float4 E, float2 f, float su,
+                                                    float sv, float w0r, float dwr, float nzm1) {
+    const float k = E.z, cm1 = E.w, fa = f.x, fb = f.y, cnt = cm1 + 1.0f;
+    const float wk = fmaf(dwr, k, w0r), wl = fmaf(dwr, cm1, wk);
+    const float kz = floorf(fminf(fmaxf(wk, -1.0f), nzm1));
+    const float kl = floorf(fminf(fmaxf(wl, -1.0f), nzm1));
+    const int nb = (int)fabsf(kl - kz);
+    const float Au = 1.0f - fa, Av = 1.0f - fb, uv = su * sv;
+    const float4 c0 = make_float4(Au * Av, fa * Av, Au * fb, fa * fb);
+    const float4 c1 = make_float4(-(Au * sv + Av * su), su * Av - fa * sv, Au * sv - su * fb,
+                                  fa * sv + fb * su);
+    const float4 c2 = make_float4(uv, -uv, -uv, uv);
+    const float sg = dwr > 0.0f ? 1.0f : -1.0f;
+    float corr = 0.0f;
+    for (int i = 0; i < nb; ++i) {
+        // boundary b between slices b-1 and b, in [0, nz-1]
+        const float b = dwr > 0.0f ? kz + 1.0f + (float)i : kz - (float)i;
+        // first sample past it (its exact position does not matter: the
+        // correction vanishes at the boundary)
+        const float tb = __fdividef(b - wk, dwr);
+        const float js = fminf(fmaxf(dwr > 0.0f ? ceilf(tb) : floorf(tb) + 1.0f, 0.0f), cnt);
+        float S0, S1, S2, S3;
+        power_sums(js, cnt, S0, S1, S2, S3);
+        const float4 P0 = moment(c0, c1, c2, S0, S1, S2), P1 = moment(c0, c1, c2, S1, S2, S3);
+        const int ibd = (int)b;
+        const bool ok = ibd >= 0 && (float)ibd <= nzm1;
+        const float4 tm = tap(ok, ibd - 1), t0 = tap(ok, ibd), tp = tap(ok, ibd + 1);
+        // sum_j q(j) sg (w_j - b) = sg (wk - b) P0 + sg dw P1
+        const float x = sg * (wk - b), y = sg * dwr;
+        const float4 P = make_float4(fmaf(x, P0.x, y * P1.x), fmaf(x, P0.y, y * P1.y),
+                                     fmaf(x, P0.z, y * P1.z), fmaf(x, P0.w, y * P1.w));
+        const float4 d2 = make_float4(tp.x + tm.x - 2.0f * t0.x, tp.y + tm.y - 2.0f * t0.y,
+                                      tp.z + tm.z - 2.0f * t0.z, tp.w + tm.w - 2.0f * t0.w);
+        corr += dot4(P, d2);
+    }
+    return corr;
+}
+
+// A shared-memory load the compiler keeps where it is written (not hoisted
+// out of a loop into a register held across it).
+__device__ __forceinline__ float4 lds_fresh(const float4 *p) {
+    float4 v;
+    asm volatile("ld.volatile.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+
+// (more rows per lane hold more accumulators: fewer blocks per SM)
+template <int RPL>
+__global__ void __launch_bounds__(CT_CONE_SEG_WARPS * 32,
+                                  RPL <= 2 ? CT_CONE_SEG_MINB : 12 - RPL * 2)
+    cone_fp_seg_kernel(const unsigned long long *__restrict__ cols, float *__restrict__ proj,
+                       const float4 *__restrict__ ray, const int *__restrict__ nsamp,
+                       const float2 *__restrict__ chan_s, const float *__restrict__ view_z,
+                       ConeFpArgs a, int nzp) {
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr int NW = CT_CONE_SEG_WARPS;
+    __shared__ SegQueue sq[NW];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    SegQueue &q = sq[wid];
+    // a block is NW adjacent channels of one view
+    // blocks channel-group-major: the resident blocks hold most views of a
+    // few channel groups
+    const int cg = blockIdx.x / a.V, v = blockIdx.x - cg * a.V;
+    const int c = cg * NW + wid;  // the warp's channel
+    if (c >= a.C) return;         // warp-uniform
+    const float zs = view_z ? __ldg(view_z + v) : 0.0f;
+    const int Q = a.nx + 1;
+    const float nzm1 = (float)(a.nz - 1);
+    const unsigned long long *pz = cols + 1;  // slice 0 of column 0
+    // the ray: steps, sample count, and per row the z cell coordinate
+    // w0 + dw k of sample k
+    const int n = __ldg(nsamp + (size_t)v * a.C + c);
+    const float mn = (float)n;
+    const float4 my = n > 0 ? __ldg(ray + (size_t)v * a.C + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 sd = n > 0 ? __ldg(chan_s + c) : make_float2(0.f, 0.f);
+    const float ds = n > 0 ? -sd.y / mn : 0.0f;
+    float w0[RPL], dw[RPL];
+#pragma unroll
+    for (int s = 0; s < RPL; ++s) {
+        const int r = lane + 32 * s;
+        const float h = a.det_bottom + a.drow * ((float)r + 0.5f);
+        const bool live = n > 0 && r < a.n_rows;
+        w0[s] = live ? (h * sd.x / a.D + zs - a.zmin) / a.dz - 0.5f : 0.0f;
+        dw[s] = live ? h * ds / (a.D * a.dz) : 0.0f;
+    }
+    // lines floor(A0) - dir .. floor(A0 + SA (n-1)) + dir of the walk's major
+    // axis hold every sample
+    int nchunk = 0;
+    if (n > 0) {
+        const bool vmaj = fabsf(my.w) >= fabsf(my.z);
+        const float A0 = (vmaj ? my.y : my.x) - 0.5f, SA = vmaj ? my.w : my.z;
+        const int dir = SA >= 0.0f ? 1 : -1;
+        const int ja = (int)floorf(A0), jb = (int)floorf(fmaf(SA, mn - 1.0f, A0));
+        nchunk = ((jb - ja) * dir + 3 + 31) / 32;
+    }
+    if (lane == 0) q.ray = my;
+
+    unsigned long long A2[RPL], M2[RPL];
+    float Cx[RPL];
+#pragma unroll
+    for (int s = 0; s < RPL; ++s) {
+        A2[s] = 0ull;
+        M2[s] = 0ull;
+        Cx[s] = 0.0f;
+    }
+    // one row's taps at a segment: slices kz and kz+1 as f32x2 pairs, its z
+    // fraction and whether its z cell may change inside the segment
+    struct RowTap {
+        unsigned long long a01, a23, c01, c23;
+        float cz;
+        bool cross;
+    };
+    auto fetch = [&](const float4 &E, int s) {
+        RowTap r;
+        const float wk = fmaf(dw[s], E.z, w0[s]);
+        const float wc = fminf(fmaxf(wk, -1.0f), nzm1);
+        const float kz = floorf(wc);
+        r.cz = wc - kz;
+        // the clamped z cell of the segment's last sample differs
+        r.cross = floorf(fminf(fmaxf(fmaf(dw[s], E.w, wk), -1.0f), nzm1)) != kz;
+        const int iz = (int)kz;
+        const unsigned long long *c0p = pz + __float_as_int(E.x);
+        const unsigned long long *c1p = pz + __float_as_int(E.y);
+        r.a01 = __ldg(c0p + iz);
+        r.a23 = __ldg(c1p + iz);
+        r.c01 = __ldg(c0p + iz + 1);
+        r.c23 = __ldg(c1p + iz + 1);
+        return r;
+    };
+    auto accumulate = [&](const RowTap &r, const float4 &W, const float4 &M, int s) {
+        const unsigned long long d01 = zt_sub2(r.c01, r.a01), d23 = zt_sub2(r.c23, r.a23);
+        const unsigned long long czp = pack2(r.cz, r.cz);
+        A2[s] = fma2(pack2(W.x, W.y), fma2(czp, d01, r.a01), A2[s]);
+        A2[s] = fma2(pack2(W.z, W.w), fma2(czp, d23, r.a23), A2[s]);
+        M2[s] = fma2(pack2(M.x, M.y), d01, M2[s]);
+        M2[s] = fma2(pack2(M.z, M.w), d23, M2[s]);
+    };
+
+    for (int ch = 0; ch < nchunk; ++ch) {
+        __syncwarp();
+        // walk: the segments of this lane's line, in (major, minor) axes
+        const float4 ry = lds_fresh(&q.ray);
+        const float u0 = ry.x - 0.5f, v0 = ry.y - 0.5f, su = ry.z, sv = ry.w;
+        const bool vmaj = fabsf(sv) >= fabsf(su);
+        const float A0 = vmaj ? v0 : u0, SA = vmaj ? sv : su;
+        const float B0 = vmaj ? u0 : v0, SB = vmaj ? su : sv;
+        const float ia = 1.0f / SA, ib = SB != 0.0f ? 1.0f / SB : 0.0f;
+        const int dir = SA >= 0.0f ? 1 : -1;
+        const float dB = SB >= 0.0f ? 1.0f : -1.0f;
+        const int ja = (int)floorf(A0), jb = (int)floorf(fmaf(SA, mn - 1.0f, A0));
+        const int J0 = ja - dir, lines = (jb - ja) * dir + 3;
+        const int m = ch * 32 + lane;
+        int ns = 0;
+        if (m < lines) {
+            const int jm = J0 + dir * m;
+            const float tA = ((float)jm - A0) * ia, tB = ((float)(jm + 1) - A0) * ia;
+            const float ka = fmaxf(0.0f, ceilf(fminf(tA, tB)));
+            const float kb = fminf(mn, ceilf(fmaxf(tA, tB)));
+            float k = ka;
+            float cb = floorf(fmaf(SB, ka, B0));
+            for (int it = 0; it <= kSegPerLane && k < kb && ns < kSegPerLane; ++it) {
+                const float bb = SB >= 0.0f ? cb + 1.0f : cb;
+                const float ke = SB != 0.0f ? fminf(kb, ceilf((bb - B0) * ib)) : kb;
+                if (ke > k) {
+                    const float cu = vmaj ? cb : (float)jm, cv = vmaj ? (float)jm : cb;
+                    const float fa = fmaf(su, k, u0) - cu, fb = fmaf(sv, k, v0) - cv;
+                    const float cnt = ke - k;
+                    const float Au = 1.0f - fa, Av = 1.0f - fb, uv = su * sv;
+                    const float4 c0 = make_float4(Au * Av, fa * Av, Au * fb, fa * fb);
+                    const float4 c1 =
+                        make_float4(-(Au * sv + Av * su), su * Av - fa * sv, Au * sv - su * fb,
+                                    fa * sv + fb * su);
+                    const float4 c2 = make_float4(uv, -uv, -uv, uv);
+                    float S0, S1, S2, S3;
+                    power_sums(0.0f, cnt, S0, S1, S2, S3);
+                    const int qi = (int)cu + 1, qj = (int)cv + 1;
+                    (void)CT_DCHECK((unsigned)qi < (unsigned)Q && (unsigned)qj < (unsigned)Q);
+                    const int xq = min(max(qi, 0), a.nx);
+                    const int off0 = (min(max(qj - 1, 0), a.ny - 1) * Q + xq) * nzp;
+                    const int off1 = (min(max(qj, 0), a.ny - 1) * Q + xq) * nzp;
+                    const int slot = lane * kSegPerLane + ns;
+                    q.e[slot] = make_float4(__int_as_float(off0), __int_as_float(off1), k,
+                                            cnt - 1.0f);
+                    q.W[slot] = moment(c0, c1, c2, S0, S1, S2);
+                    q.M[slot] = moment(c0, c1, c2, S1, S2, S3);
+                    q.f[slot] = make_float2(fa, fb);
+                    ++ns;
+                    k = ke;
+                }
+                cb += dB;
+            }
+        }
+        __syncwarp();
+        // drain: every queued segment for every row
+        unsigned xm[RPL][kSegPerLane];
+#pragma unroll
+        for (int t = 0; t < kSegPerLane; ++t) {
+#pragma unroll
+            for (int s = 0; s < RPL; ++s) xm[s][t] = 0u;
+            unsigned mask = __ballot_sync(FULL, ns > t);
+            while (mask) {
+                const int L = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int e = L * kSegPerLane + t;
+                const float4 E = q.e[e];
+                RowTap r[RPL];
+#pragma unroll
+                for (int s = 0; s < RPL; ++s) r[s] = fetch(E, s);
+                const float4 W = q.W[e], M = q.M[e];
+#pragma unroll
+                for (int s = 0; s < RPL; ++s) {
+                    accumulate(r[s], W, M, s);
+                    xm[s][t] |= r[s].cross ? 1u << L : 0u;
+                }
+            }
+        }
+        // crossings: each lane works through its marked (segment, row) pairs
+        for (;;) {
+            bool have = false;
+            int ps = 0, pt = 0;
+            unsigned bits = 0u;
+#pragma unroll
+            for (int s = 0; s < RPL; ++s)
+#pragma unroll
+                for (int t = 0; t < kSegPerLane; ++t)
+                    if (!have && xm[s][t]) {
+                        have = true;
+                        ps = s;
+                        pt = t;
+                        bits = xm[s][t];
+                    }
+            if (!__any_sync(FULL, have)) break;
+            if (have) {
+                const int L = __ffs(bits) - 1;
+                float w0r = 0.0f, dwr = 0.0f;
+#pragma unroll
+                for (int s = 0; s < RPL; ++s) {
+#pragma unroll
+                    for (int t = 0; t < kSegPerLane; ++t)
+                        if (s == ps && t == pt) xm[s][t] &= xm[s][t] - 1u;
+                    if (s == ps) {
+                        w0r = w0[s];
+                        dwr = dw[s];
+                    }
+                }
+                const int e = L * kSegPerLane + pt;
+                const float4 E = q.e[e];
+                const unsigned long long *c0p = pz + __float_as_int(E.x);
+                const unsigned long long *c1p = pz + __float_as_int(E.y);
+                auto tap = [&](bool ok, int z) {
+                    const float2 lo = zt_unpack(CT_DLOAD(ok, c0p + z));
+                    const float2 hi = zt_unpack(CT_DLOAD(ok, c1p + z));
+                    return make_float4(lo.x, lo.y, hi.x, hi.y);
+                };
+                const float4 ry = lds_fresh(&q.ray);
+                const float corr = cone_seg_crossings(tap, E, q.f[e], ry.z, ry.w, w0r, dwr, nzm1);
+#pragma unroll
+                for (int s = 0; s < RPL; ++s)
+                    if (s == ps) Cx[s] += corr;
+            }
+        }
+        __syncwarp();  // the queue is rewritten by the next chunk
+    }
+#pragma unroll
+    for (int s = 0; s < RPL; ++s) {
+        const int r = lane + 32 * s;
+        if (r >= a.n_rows) continue;
+        const float h = a.det_bottom + a.drow * ((float)r + 0.5f);
+        const float2 av = unpack2(A2[s]), mv = unpack2(M2[s]);
+        const float val = (av.x + av.y) + Cx[s] + dw[s] * (mv.x + mv.y);
+        proj[((size_t)v * a.n_rows + r) * a.C + c] = val * a.w * sqrtf(1.0f + (h / a.D) * (h / a.D));
+    }
+}
+
 ConeArgs make_cone_args(const ct_plan *p) {
     ConeArgs a;
     a.V = p->g.n_views;
@@ -1234,10 +1593,25 @@ int cone_bp_transpose(const ct_plan *p, const float *vol, float *proj, int batch
     return (int)cudaGetLastError();
 }
 
+// Up to 128 detector rows the single-walk projector runs (its rows are lanes
+// of one warp, four per lane at most); taller detectors use the row-group one.
+#ifndef CT_CONE_FP_WALK_ROWS
+#define CT_CONE_FP_WALK_ROWS 128
+#endif
+// (column offsets are int32)
+static bool cone_fp_single_walk(const ct_plan *p) {
+    const double cells = (double)(p->g.nx + 1) * (double)(p->g.nx + 1) * (double)(p->nz + 2);
+    return p->n_rows <= (CT_CONE_FP_WALK_ROWS < 128 ? CT_CONE_FP_WALK_ROWS : 128) &&
+           cells < 2147483647.0;
+}
+
 size_t cone_fp_work_bytes(const ct_plan *p, int batch) {
-    // the quad images of one volume at a time
+    // the quad images of one volume at a time: z-major columns of slices
+    // -1 .. nz for the single-walk projector, two layouts per slice otherwise
     (void)batch;
-    return sizeof(float4) * 2 * (size_t)p->nz * (p->g.nx + 1) * (p->g.nx + 1);
+    const size_t cells = (size_t)(p->g.nx + 1) * (p->g.nx + 1);
+    if (!cone_fp_single_walk(p)) return sizeof(float4) * 2 * (size_t)p->nz * cells;
+    return sizeof(float2) * (size_t)(p->nz + 2) * (p->g.nx + 1) * p->g.ny;
 }
 
 int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *work,
@@ -1249,6 +1623,7 @@ int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *wo
     a.V = p->g.n_views;
     a.C = p->g.n_cols;
     a.nx = nx;
+    a.ny = ny;
     a.nz = nz;
     a.n_rows = p->n_rows;
     a.wpv = (a.C + 31) / 32;
@@ -1259,10 +1634,31 @@ int cone_fp(const ct_plan *p, const float *vol, float *proj, int batch, void *wo
     a.dz = p->g.dz;
     a.zmin = -0.5f * p->g.dz * (float)nz;
     a.max_iter = 2 * (nx > ny ? nx : ny) + 8;
+    const int Q = nx + 1;
+    if (cone_fp_single_walk(p)) {
+        constexpr int CPB = CT_CONE_SEG_WARPS;
+        const int nzp = nz + 2;
+        const int rpl = (a.n_rows + 31) / 32;
+        auto kern = rpl == 1   ? cone_fp_seg_kernel<1>
+                    : rpl == 2 ? cone_fp_seg_kernel<2>
+                    : rpl == 3 ? cone_fp_seg_kernel<3>
+                               : cone_fp_seg_kernel<4>;
+        const unsigned blocks = (unsigned)((a.C + CPB - 1) / CPB) * (unsigned)a.V;
+        for (int b = 0; b < batch; ++b) {
+            cone_pairs_z_kernel<<<dim3((Q + 31) / 32, ny, (nzp + 31) / 32), dim3(32, 8), 0, s>>>(
+                vol + (size_t)b * nz * nx * ny, reinterpret_cast<float2 *>(work), nx, ny, nz,
+                nzp);
+            kern<<<blocks, CT_CONE_SEG_WARPS * 32, 0, s>>>(
+                static_cast<const unsigned long long *>(work), proj + (size_t)b * a.V * a.n_rows * a.C,
+                reinterpret_cast<const float4 *>(p->d_ray), p->d_nsamp,
+                reinterpret_cast<const float2 *>(p->d_chan_s), p->d_view_z, a, nzp);
+            ct_count_launch(2);
+        }
+        return (int)cudaGetLastError();
+    }
     constexpr int RB = CT_CONE_FP_ROWS;
     const int rgroups = (a.n_rows + RB - 1) / RB;
     const int blocks = (a.V + kConeFpThreads / 32 - 1) / (kConeFpThreads / 32) * a.wpv;
-    const int Q = nx + 1;
     for (int b = 0; b < batch; ++b) {
         cone_quads_kernel<<<dim3((Q + 31) / 32, (Q + 7) / 8, 2 * nz), dim3(32, 8), 0, s>>>(
             vol + (size_t)b * nz * nx * ny, quads, nx, ny);

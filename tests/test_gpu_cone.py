@@ -203,3 +203,20 @@ def test_cone_full_size_properties(cuda):
     p2 = plan.fp_cone(v1[1:2])
     assert torch.equal(p2[0], p1[1])
     assert rel_l2(_np(plan.fp_cone(3.0 * v1)), 3.0 * _np(p1)) < 1e-6
+
+
+@pytest.mark.parametrize("n_rows", [40, 80, 128, 136])
+def test_cone_fp_detector_heights(cuda, orc, n_rows):
+    """The cone FP at 1 .. 4 detector rows per lane of the single-walk
+    projector (40, 80, 128 rows) and past it (136 rows: the row-group
+    projector), on the same 72 mm detector, against the oracle; rows cross
+    several slices per segment at this cone angle."""
+    p, a, nr, nz = G.cone_small(n=32, views=24, cols=48, n_rows=n_rows, nz=12,
+                                drow=72.0 / n_rows)
+    plan = ConePlan(p, a, nr, nz, device=cuda)
+    g = orc.decode(p)
+    x = _vol(g, nz, 1, seed=7)
+    got = _np(plan.fp_cone(_t(x, cuda)))
+    ref = orc.cone_fp(g, nr, nz, a, x)
+    assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
+    assert torch.equal(plan.fp_cone(_t(x, cuda)), plan.fp_cone(_t(x, cuda)))
