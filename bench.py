@@ -762,6 +762,16 @@ def main() -> None:
                 "fp_cone_ms_per_volume": t_fp, "fdk_ms_per_volume": t_fdk,
                 "fdk_adjoint_ms_per_volume": t_adj,
                 "fdk_gvoxel_views_per_s": 512 * 512 * 64 * VIEWS / t_fdk / 1e6}
+        # the cone FP's in-plane cells are the fan FP's (same rays): 8 FP32 taps per
+        # (cell, detector row)
+        cone_l1 = 32.0 * 64 * visits
+        cone_ach = cone_l1 / (t_fp * 1e-3) / 1e9
+        cone["fp_roofline"] = {
+            "bound": "l1", "kernel": "cone_fp_seg_kernel", "achieved": cone_ach,
+            "peak": pk["l1_load_gbs"], "unit": "GB/s", "frac": cone_ach / pk["l1_load_gbs"],
+            "algorithmic": (f"32 B (eight FP32 trilinear taps) per (in-plane cell, detector row) x "
+                            f"{visits} cells x 64 rows = {cone_l1:.4g} B per volume"),
+            "timed": "per-volume CUDA events of ct_fp_cone (its column build included)"}
         del cvol, cproj, crec, cgrad
         cplan.close()
 
