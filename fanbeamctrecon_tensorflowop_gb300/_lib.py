@@ -113,6 +113,7 @@ SIGNATURES = {
     "ct_build_flags": (ctypes.c_uint32, []),
     "ct_set_allocator": (_i, [_P(CtAllocator)]),
     "ct_device_alloc_count": (ctypes.c_uint64, []),
+    "ct_host_mapped": (_i, [_vp, _P(_vp)]),
     "ct_geom_from_param16": (_i, [_P(ctypes.c_float), _P(CtFanGeom)]),
     "ct_fp_ray_table": (_i, [_P(CtFanGeom), _P(ctypes.c_float), _i, _P(ctypes.c_float),
                             _P(ctypes.c_int32)]),

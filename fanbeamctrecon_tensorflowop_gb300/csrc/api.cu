@@ -308,6 +308,24 @@ ct_status ct_set_allocator(const ct_allocator *allocator) {
 
 uint64_t ct_device_alloc_count(void) { return g_alloc_count.load(std::memory_order_relaxed); }
 
+ct_status ct_host_mapped(const void *host_ptr, void **device_ptr) {
+    if (!host_ptr || !device_ptr) return CT_ERR_NULL_POINTER;
+    *device_ptr = nullptr;
+    cudaPointerAttributes at;
+    const cudaError_t e = cudaPointerGetAttributes(&at, host_ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // an unknown pointer leaves no error on the context
+        g_last_error = "ct_host_mapped: not CUDA host memory";
+        return CT_ERR_INVALID_ARGUMENT;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) {
+        g_last_error = "ct_host_mapped: not page-locked host memory mapped for the device";
+        return CT_ERR_INVALID_ARGUMENT;
+    }
+    *device_ptr = at.devicePointer;
+    return CT_OK;
+}
+
 ct_status ct_geom_from_param16(const float param[16], ct_fan_geom *out) {
     return ct_decode_param16(param, out);
 }

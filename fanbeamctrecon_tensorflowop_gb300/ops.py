@@ -149,6 +149,26 @@ class FanPlan:
         x = self._check_in(img, self.image_shape, "image")
         return self._run("ct_fp_fan", _lib.OP_FP, x, self.sino_shape, True, out)
 
+    def fp_to_host(self, img: torch.Tensor) -> torch.Tensor:
+        """``fp`` with its sinogram written straight into page-locked host memory:
+        the kernel's stores cross to the host while it runs and no device-to-host
+        copy follows.  Returns a pinned CPU tensor, complete once the device's
+        current stream has been synchronised."""
+        x = self._check_in(img, self.image_shape, "image")
+        host = torch.empty((x.shape[0], *self.sino_shape), dtype=torch.float32, pin_memory=True)
+        dptr = ctypes.c_void_p()
+        st = self._lib.ct_host_mapped(ctypes.c_void_p(host.data_ptr()), ctypes.byref(dptr))
+        if st != 0:
+            # page-locked memory that is not mapped for the device: copy back instead
+            return self.fp(x).to("cpu")
+        B = x.shape[0]
+        with torch.cuda.device(self.device):
+            work, nbytes = self._work(_lib.OP_FP, B)
+            st = self._lib.ct_fp_fan(self._h, _ptr(x), dptr.value, B, _ptr(work), nbytes,
+                                     self._stream())
+        _lib.check(st, "ct_fp_fan")
+        return host
+
     def fp_adjoint(self, sino: torch.Tensor, out=None) -> torch.Tensor:
         """Exact transpose of ``fp``."""
         y = self._check_in(sino, self.sino_shape, "sinogram")

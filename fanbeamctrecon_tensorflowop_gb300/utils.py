@@ -96,6 +96,16 @@ def _run(op: str, x, angle_arr, parameter, vol_shape, proj_shape, window: int):
         xin, kind = _to_device(x, plan.sino_shape, device)
         out_shape = tuple(int(s) for s in vol_shape)
     grad = kind == "cuda" and torch.is_grad_enabled() and x.requires_grad
+    if op == "fp" and kind != "cuda":
+        # host caller: the projector writes the sinogram into page-locked host
+        # memory as it runs
+        host = plan.fp_to_host(xin)
+        if _prod(out_shape) != host.numel():
+            raise ValueError(f"output shape {out_shape} does not hold {host.numel()} elements "
+                             f"({host.shape[0]} slices)")
+        torch.cuda.current_stream(device).synchronize()
+        host = host.reshape(out_shape)
+        return host.numpy() if kind == "numpy" else host
     if op == "fp":
         y = autograd.forward_project(xin, plan) if grad else plan.fp(xin)
     elif op == "bp":

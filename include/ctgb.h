@@ -200,6 +200,16 @@ ct_status ct_set_allocator(const ct_allocator *allocator);
  * either route (ct_set_allocator's or the CUDA runtime's). */
 uint64_t ct_device_alloc_count(void);
 
+/* Whether host_ptr lies in page-locked host memory mapped into the current
+ * device's address space; if so *device_ptr receives the address kernels use
+ * for it (the same value under unified addressing).  An operator may then
+ * write its output there directly: ct_fp_fan stores every output element
+ * exactly once, so its sinogram crosses to the host while it runs and no
+ * device-to-host copy follows.  CT_ERR_INVALID_ARGUMENT for pageable or
+ * unmapped memory.  No counterpart in the reference (its ops returned TF
+ * tensors). */
+ct_status ct_host_mapped(const void *host_ptr, void **device_ptr);
+
 /* ---- geometry ------------------------------------------------------------ */
 
 /* Decodes the 16-float parameter vector.  Replaces the attr decoding of
