@@ -869,9 +869,13 @@ def main() -> None:
     # ---- e2e through the reference-named entry point with host buffers ---------------
     host_imgs = [imgs[k].cpu().numpy() for k in range(2)]
     vs, ps = [BATCH, N_PIX, N_PIX], [BATCH, VIEWS, COLS]
-    for k in range(args.warmup):
-        utils.fp_fan_curve(volume=host_imgs[k % 2], angle=a, parameter=p, vol_shape=vs,
-                           proj_shape=ps)
+    # the warm-up holds each result while the next call runs, as the timed loop
+    # does, so the page-locked result buffers it cycles through already exist
+    out = None
+    for k in range(max(args.warmup, 3)):
+        out = utils.fp_fan_curve(volume=host_imgs[k % 2], angle=a, parameter=p, vol_shape=vs,
+                                 proj_shape=ps)
+    del out
     barrier()
     n_e2e = max(5, args.steps // 3)
     t0 = time.perf_counter()
