@@ -15,8 +15,9 @@ plain per-view launch loop on the same GPU, cone beam and uneven batches.
 Roofline: the interpolation kernels are bound by the L1 data path (their
 gathers hit L1), so ``roofline`` sets the forward projector's algorithmic L1
 load bytes -- one 16-byte quad per (ray, cell) visit and slice -- against the
-L1 load peak that ``csrc/peaks`` measures in this same run; the compulsory
-and the measured DRAM traffic are reported beside it.
+L1 load peak that ``csrc/peaks`` measures in this same run (the faster of
+coalesced 16- and 32-byte loads); the compulsory and the measured DRAM
+traffic are reported beside it.
 
 ``cpu_baseline`` and ``--impl reference`` time the reference's algorithms on
 the host cores as an FP32 OpenMP transcription (oracle/cpu_fp32.c).  The
@@ -62,6 +63,8 @@ QUAD_BYTES = 16      # FP: one float4 of four clamped taps per (ray, cell) visit
 TAP_BYTES = 8        # BP: two FP32 taps per pixel-view and slice (a 16-byte pair per 2 slices)
 SINO_BYTES = 4       # FP adjoint: one FP32 sinogram value per (cell, ray) pair and slice
 FMA_FLOP_PER_VISIT = 8  # FP: per visit and slice, two f32x2 FMAs (w . taps)
+L1_PEAK_SOURCE = ("measured in this run (csrc/peaks): the larger of the coalesced 16-byte and "
+                  "32-byte L1-hit load rates (peaks.l1_load_gbs, peaks.l1_load32_gbs)")
 
 
 def c1_geometry():
@@ -194,6 +197,7 @@ def measure_peaks(gpu_index: int) -> dict:
     lib = ctypes.CDLL(str(_build.PEAKS_PATH))
     d = ctypes.c_double
     lib.ctpk_l1_load.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(d), ctypes.POINTER(d)]
+    lib.ctpk_l1_load_v8.argtypes = lib.ctpk_l1_load.argtypes
     lib.ctpk_fma.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(d),
                              ctypes.POINTER(d)]
     lib.ctpk_sm_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
@@ -202,14 +206,15 @@ def measure_peaks(gpu_index: int) -> dict:
         raise RuntimeError("ctpk_sm_count failed")
     out = {"sm_count": sms.value}
     with ClockSampler(gpu_index) as clk:
-        best = 0.0
-        for _ in range(3):
-            v, ms = d(), d()
-            rc = lib.ctpk_l1_load(4, 2000, ctypes.byref(v), ctypes.byref(ms))
-            if rc:
-                raise RuntimeError(f"ctpk_l1_load failed: CUDA error {rc}")
-            best = max(best, v.value)
-        out["l1_load_gbs"] = best
+        for fn, key in ((lib.ctpk_l1_load, "l1_load_gbs"), (lib.ctpk_l1_load_v8, "l1_load32_gbs")):
+            best = 0.0
+            for _ in range(3):
+                v, ms = d(), d()
+                rc = fn(4, 2000, ctypes.byref(v), ctypes.byref(ms))
+                if rc:
+                    raise RuntimeError(f"L1 load peak failed: CUDA error {rc}")
+                best = max(best, v.value)
+            out[key] = best
         for packed, key in ((0, "fp32_tflops_scalar"), (1, "fp32_tflops_f32x2")):
             best = 0.0
             for _ in range(3):
@@ -224,9 +229,12 @@ def measure_peaks(gpu_index: int) -> dict:
     out["clocks"] = c
     if c.get("sm_mhz"):
         out["l1_bytes_per_clk_per_sm"] = out["l1_load_gbs"] * 1e9 / (c["sm_mhz"] * 1e6) / sms.value
-    out["how"] = ("csrc/peaks: L1 = 16-byte ld.global.nc over a 32 KiB per-SM buffer, 4 x 512 "
-                  "threads per SM; FP32 = 8 independent FMA chains per thread, scalar and f32x2; "
-                  "best of 3 launches, CUDA events")
+        out["l1_32b_bytes_per_clk_per_sm"] = (out["l1_load32_gbs"] * 1e9 / (c["sm_mhz"] * 1e6)
+                                              / sms.value)
+    out["how"] = ("csrc/peaks: L1 = 16-byte (ld.global.nc.v4.f32) and 32-byte "
+                  "(ld.global.nc.v8.f32) loads over a 32 KiB per-SM buffer, adjacent lanes on "
+                  "adjacent addresses, 4 x 512 threads per SM; FP32 = 8 independent FMA chains "
+                  "per thread, scalar and f32x2; best of 3 launches, CUDA events")
     return out
 
 
@@ -590,6 +598,9 @@ def main() -> None:
     # ---- peaks of this GPU, measured now (untimed) ----------------------------------
     pk = measure_peaks(smi)
     hbm = measured_peaks()
+    # the L1 load path's peak: 32-byte loads move about twice the bytes of
+    # 16-byte ones in the same time, so the larger of the two is the roofline
+    l1_peak = max(pk["l1_load_gbs"], pk["l1_load32_gbs"])
 
     # ---- headline: FP throughput -----------------------------------------------
     def fp_step(k):
@@ -612,9 +623,10 @@ def main() -> None:
     traffic = profiled("fp_fan_kernel", "dram_bytes_per_launch")
     compulsory = 4.0 * (N_PIX * N_PIX + VIEWS * COLS) * BATCH
     roofline = {
-        "bound": "l1", "achieved": achieved, "peak": pk["l1_load_gbs"], "unit": "GB/s",
-        "frac": achieved / pk["l1_load_gbs"], "traffic": traffic,
-        "peak_source": "measured in this run (csrc/peaks: coalesced 16-byte L1-hit loads)",
+        "bound": "l1", "achieved": achieved, "peak": l1_peak, "unit": "GB/s",
+        "frac": achieved / l1_peak, "traffic": traffic,
+        "peak_source": L1_PEAK_SOURCE,
+        "frac_of_16b_load_peak": achieved / pk["l1_load_gbs"],
         "kernel": "fp_fan_kernel",
         "algorithmic": (f"{QUAD_BYTES} B (one float4 quad) per (ray, cell) visit and slice x "
                         f"{visits} visits per slice x {BATCH} slices = {l1_bytes:.4g} B per launch"),
@@ -645,8 +657,8 @@ def main() -> None:
     bp_s = sum(per_bp) / len(per_bp) * bp_share
     bp_bytes = TAP_BYTES * BATCH * fovpix * VIEWS
     bp_roof = {"bound": "l1", "kernel": "bp_fan_kernel", "achieved": bp_bytes / bp_s / 1e9,
-               "peak": pk["l1_load_gbs"], "unit": "GB/s",
-               "frac": bp_bytes / bp_s / 1e9 / pk["l1_load_gbs"],
+               "peak": l1_peak, "unit": "GB/s",
+               "frac": bp_bytes / bp_s / 1e9 / l1_peak, "peak_source": L1_PEAK_SOURCE,
                "algorithmic": (f"{TAP_BYTES} B (two FP32 taps) per in-FOV pixel-view and slice "
                                f"x {fovpix} pixels x {VIEWS} views x {BATCH} slices"),
                "share_of_step": bp_share,
@@ -693,8 +705,8 @@ def main() -> None:
     adj_s = sum(per_adj) / len(per_adj) * adj_share
     adj_bytes = SINO_BYTES * BATCH * visits
     adj_roof = {"bound": "issue", "kernel": "fp_adjoint_cells_kernel",
-                "achieved": adj_bytes / adj_s / 1e9, "peak": pk["l1_load_gbs"], "unit": "GB/s",
-                "frac": adj_bytes / adj_s / 1e9 / pk["l1_load_gbs"],
+                "achieved": adj_bytes / adj_s / 1e9, "peak": l1_peak, "unit": "GB/s",
+                "frac": adj_bytes / adj_s / 1e9 / l1_peak, "peak_source": L1_PEAK_SOURCE,
                 "algorithmic": (f"{SINO_BYTES} B (one FP32 sinogram value) per (cell, ray) pair "
                                 f"and slice x {visits} pairs per slice x {BATCH} slices"),
                 "share_of_step": adj_share}
@@ -768,7 +780,8 @@ def main() -> None:
         cone_ach = cone_l1 / (t_fp * 1e-3) / 1e9
         cone["fp_roofline"] = {
             "bound": "l1", "kernel": "cone_fp_seg_kernel", "achieved": cone_ach,
-            "peak": pk["l1_load_gbs"], "unit": "GB/s", "frac": cone_ach / pk["l1_load_gbs"],
+            "peak": l1_peak, "unit": "GB/s", "frac": cone_ach / l1_peak,
+            "peak_source": L1_PEAK_SOURCE,
             "algorithmic": (f"32 B (eight FP32 trilinear taps) per (in-plane cell, detector row) x "
                             f"{visits} cells x 64 rows = {cone_l1:.4g} B per volume"),
             "timed": "per-volume CUDA events of ct_fp_cone (its column build included)"}

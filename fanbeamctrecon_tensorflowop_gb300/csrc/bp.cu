@@ -17,6 +17,8 @@
 // accuracy, 3e-8 absolute), with atanf kept for fans wider than 90 degrees.
 // Plans with texture_weights = 1 round the interpolation weight as the
 // reference's texture unit does (tex_weight); the default keeps exact FP32.
+#include <cstdint>
+
 #include "bp_body.cuh"
 
 namespace ctk {
@@ -247,7 +249,8 @@ size_t bp_fan_work_bytes(const ct_plan *p, int batch) {
     if (!sb) return 0;
     const int per = batch < kPairSlices ? batch : kPairSlices;
     const int groups = (per + sb - 1) / sb;
-    return sizeof(float4) * (sb / 2) * (size_t)groups * p->g.n_views * (p->g.n_cols + 1);
+    // + 16 bytes to start the 32-byte entries on a 32-byte boundary
+    return sizeof(float4) * (sb / 2) * (size_t)groups * p->g.n_views * (p->g.n_cols + 1) + 16;
 }
 
 int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weighted, void *work,
@@ -258,7 +261,9 @@ int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weigh
     const bool tex = p->opts.texture_weights != 0;
     const size_t slice = (size_t)a.V * a.C, plane = (size_t)a.nx * a.ny;
     if (const int sb = work ? pair_group(batch) : 0) {
-        float4 *pairs = static_cast<float4 *>(work);
+        // 32-byte entries read by 32-byte loads (the workspace is 16-byte aligned)
+        float4 *pairs = reinterpret_cast<float4 *>((reinterpret_cast<uintptr_t>(work) + 31) &
+                                                   ~(uintptr_t)31);
         for (int b0 = 0; b0 < batch; b0 += kPairSlices) {
             const int nb = batch - b0 < kPairSlices ? batch - b0 : kPairSlices;
             const int groups = (nb + sb - 1) / sb;

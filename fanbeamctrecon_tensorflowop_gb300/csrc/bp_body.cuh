@@ -57,9 +57,10 @@ __device__ __forceinline__ float tex_weight(float f) {
 // Block of 32 x 8 threads, ROWS pixels per thread (32 x 32 tiles by default);
 // block-uniform call.  TEX: texture-unit weights (tex_weight) instead of
 // exact FP32 ones.  PAIRS (SB = 4 or 8): the taps come from the slice group's
-// tap image `pairs` ([V][C+1] x SB/2 float4: for column position i, the
-// clamped taps (i0, i1) of slices 0..SB-1), SB/2 16-byte loads per pixel-view
-// instead of 2 SB 4-byte gathers; same values, same arithmetic.
+// tap image `pairs` ([V][C+1] x SB/2 float4, 32-byte aligned: for column
+// position i, the clamped taps (i0, i1) of slices 0..SB-1), SB/4 32-byte
+// loads per pixel-view instead of 2 SB 4-byte gathers; same values, same
+// arithmetic.
 template <bool WEIGHTED, int SB, int DEG, typename OutT, int ROWS = kBpRowsPerThr,
           bool TEX = false, bool PAIRS = false>
 __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t sstride,
@@ -112,13 +113,17 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
                     if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));
                     float v0[SB], v1[SB];
                     if constexpr (PAIRS) {
+                        // one 32-byte load per four slices (the entries are 32-byte aligned)
                         const float4 *q = pairs + ((size_t)v * (a.C + 1) + i) * (SB / 2);
                         const bool ok = (unsigned)i <= (unsigned)a.C;
 #pragma unroll
-                        for (int h = 0; h < SB / 2; ++h) {
-                            const float4 t = CT_DLOAD(ok, q + h);
-                            v0[2 * h] = t.x, v1[2 * h] = t.y, v0[2 * h + 1] = t.z,
-                                     v1[2 * h + 1] = t.w;
+                        for (int h = 0; h < SB / 4; ++h) {
+                            float4 t, u;
+                            ldg_v8(ok, q + 2 * h, t, u);
+                            v0[4 * h] = t.x, v1[4 * h] = t.y, v0[4 * h + 1] = t.z,
+                                     v1[4 * h + 1] = t.w;
+                            v0[4 * h + 2] = u.x, v1[4 * h + 2] = u.y, v0[4 * h + 3] = u.z,
+                                         v1[4 * h + 3] = u.w;
                         }
                     } else {
                         const bool ok = (unsigned)i0 < (unsigned)a.C && (unsigned)i1 < (unsigned)a.C;

@@ -14,6 +14,25 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// 32 bytes at p (32-byte aligned) as two float4, one ld.global.nc.v8.f32
+// (sm_100 and later).  When adjacent lanes read adjacent 32-byte entries the
+// L1 load path completes it in about the time of one 16-byte load (measured:
+// 148 against 78 TB/s of L1 hits), so such a gather costs half the load
+// instructions of two 16-byte ones.  Gathers whose lanes scatter over many
+// lines gain nothing (the forward projector's quads and its adjoint's
+// sinogram measured slower with it).  `ok` is the debug build's index check
+// (both halves read zero when it fails).
+__device__ __forceinline__ void ldg_v8(bool ok, const float4 *p, float4 &a, float4 &b) {
+    if (CT_DCHECK(ok)) {
+        asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+            : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z),
+              "=f"(b.w)
+            : "l"(p));
+    } else {
+        a = b = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
 // Bilinear sample of a row-major [ny][nx] image at texture coordinates (x, y)
 // -- texel (i, j) centred at (i + 1/2, j + 1/2) -- with clamp-to-edge
 // addressing: the semantics of tex2D on a cudaFilterModeLinear,

@@ -7,6 +7,8 @@
 //     ld.global.nc.v4 the kernels issue) over a 32 KiB buffer that stays
 //     resident in each SM's L1; adjacent lanes read adjacent 16 bytes, so a
 //     warp's load is four full 128-byte lines, the best case of the L1 path.
+//   - ctpk_l1_load_v8: the same with 32-byte loads (ld.global.nc.v8.f32,
+//     sm_100 and later), a warp's load eight full lines.
 //   - ctpk_fma: independent FP32 FMA chains, scalar (fma.rn.f32) or packed
 //     (fma.rn.f32x2), the FP32 pipe's peak.
 // Both time one launch with CUDA events on the legacy default stream after a
@@ -30,6 +32,14 @@ __device__ __forceinline__ float4 ld_nc(const float4 *p) {
     return v;
 }
 
+// 32 bytes at p (32-byte aligned): two float4 halves.
+__device__ __forceinline__ void ld_nc8(const float4 *p, float4 &a, float4 &b) {
+    asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z),
+                   "=f"(b.w)
+                 : "l"(p));
+}
+
 // Each iteration a warp reads 8 x 512 contiguous bytes; the window moves by
 // 32 float4 per iteration, so no load repeats an address of the previous
 // iteration (the volatile loads are never merged or hoisted either).
@@ -50,6 +60,28 @@ __global__ void __launch_bounds__(512) l1_load_kernel(const float4 *__restrict__
     }
     // the buffer holds zeros: this store never happens, but the compiler
     // cannot know it, so every load stays
+    if (acc.x + acc.y + acc.z + acc.w != 0.0f) sink[blockIdx.x * blockDim.x + threadIdx.x] = acc.x;
+}
+
+// 32-byte loads: each iteration a warp reads 8 x 1024 contiguous bytes (pairs
+// of float4), the window moving by 32 pairs per iteration.
+__global__ void __launch_bounds__(512) l1_load8_kernel(const float4 *__restrict__ buf, int iters,
+                                                       float *__restrict__ sink) {
+    constexpr int kPairs = kL1Vec / 2;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    int idx = threadIdx.x;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            float4 a, b;
+            ld_nc8(buf + 2 * ((idx + k * 512) & (kPairs - 1)), a, b);
+            acc.x += a.x + b.x;
+            acc.y += a.y + b.y;
+            acc.z += a.z + b.z;
+            acc.w += a.w + b.w;
+        }
+        idx = (idx + 32) & (kPairs - 1);
+    }
     if (acc.x + acc.y + acc.z + acc.w != 0.0f) sink[blockIdx.x * blockDim.x + threadIdx.x] = acc.x;
 }
 
@@ -116,16 +148,7 @@ int time_launch(F &&launch, float *ms) {
     return (int)e;
 }
 
-}  // namespace
-
-extern "C" {
-
-// Number of SMs of the current device.
-int ctpk_sm_count(int *out) { return sm_count(out); }
-
-// L1 load bandwidth of the current device: bytes loaded by all threads /
-// launch time, in GB/s (1e9 B/s).  blocks_per_sm blocks of 512 threads per SM.
-int ctpk_l1_load(int blocks_per_sm, int iters, double *gbs, double *ms_out) {
+int l1_load(int bytes_per_load, int blocks_per_sm, int iters, double *gbs, double *ms_out) {
     int sms = 0;
     int rc = sm_count(&sms);
     if (rc) return rc;
@@ -140,14 +163,39 @@ int ctpk_l1_load(int blocks_per_sm, int iters, double *gbs, double *ms_out) {
     }
     cudaMemset(buf, 0, kL1Bytes);
     float ms = 0.0f;
-    rc = time_launch([&] { l1_load_kernel<<<blocks, 512>>>(buf, iters, sink); }, &ms);
+    rc = time_launch(
+        [&] {
+            if (bytes_per_load == 32)
+                l1_load8_kernel<<<blocks, 512>>>(buf, iters, sink);
+            else
+                l1_load_kernel<<<blocks, 512>>>(buf, iters, sink);
+        },
+        &ms);
     cudaFree(buf);
     cudaFree(sink);
     if (rc) return rc;
-    const double bytes = 16.0 * 8.0 * (double)iters * 512.0 * (double)blocks;
+    const double bytes = (double)bytes_per_load * 8.0 * (double)iters * 512.0 * (double)blocks;
     *gbs = bytes / ((double)ms * 1e-3) / 1e9;
     *ms_out = ms;
     return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Number of SMs of the current device.
+int ctpk_sm_count(int *out) { return sm_count(out); }
+
+// L1 load bandwidth of the current device: bytes loaded by all threads /
+// launch time, in GB/s (1e9 B/s).  blocks_per_sm blocks of 512 threads per SM.
+int ctpk_l1_load(int blocks_per_sm, int iters, double *gbs, double *ms_out) {
+    return l1_load(16, blocks_per_sm, iters, gbs, ms_out);
+}
+
+// The same with 32-byte loads.
+int ctpk_l1_load_v8(int blocks_per_sm, int iters, double *gbs, double *ms_out) {
+    return l1_load(32, blocks_per_sm, iters, gbs, ms_out);
 }
 
 // FP32 FMA throughput of the current device in TFLOP/s (an FMA = 2 FLOP);
