@@ -60,7 +60,7 @@ POOL = 4
 WORKLOAD = ("fan-beam FP, batch of 32 seeded ellipse phantoms 512x512 @0.7 mm, "
             "984 views x 888 equiangular channels (1 mm pitch), SID 541 / SDD 949 mm")
 QUAD_BYTES = 16      # FP: one float4 of four clamped taps per (ray, cell) visit and slice
-TAP_BYTES = 8        # BP: two FP32 taps per pixel-view and slice (a 16-byte pair per 2 slices)
+TAP_BYTES = 8        # BP: two FP32 taps per pixel-view and slice (a 32-byte entry per 4 slices)
 SINO_BYTES = 4       # FP adjoint: one FP32 sinogram value per (cell, ray) pair and slice
 FMA_FLOP_PER_VISIT = 8  # FP: per visit and slice, two f32x2 FMAs (w . taps)
 L1_PEAK_SOURCE = ("measured in this run (csrc/peaks): the larger of the coalesced 16-byte and "

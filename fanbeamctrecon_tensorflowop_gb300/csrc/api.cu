@@ -35,6 +35,11 @@ cudaError_t dev_alloc(const ct_allocator &a, void **p, size_t bytes, cudaStream_
     if (a.alloc) {
         *p = a.alloc(a.ctx, bytes, reinterpret_cast<ct_stream>(s));
         if (!*p) return cudaErrorMemoryAllocation;
+        if (reinterpret_cast<uintptr_t>(*p) % 256) {  // the documented alignment
+            a.free(a.ctx, *p, reinterpret_cast<ct_stream>(s));
+            *p = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
     } else {
         cudaError_t e = stream_ordered ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
         if (e != cudaSuccess) {
@@ -187,7 +192,7 @@ size_t op_workspace(const ct_plan *p, ct_op op, int batch) {
 void free_plan(ct_plan *p) {
     if (!p) return;
     for (void *t : {(void *)p->d_view_cs, (void *)p->d_view_cs_lo, (void *)p->d_col_tan,
-                    (void *)p->d_ray, (void *)p->d_ray_inv,
+                    (void *)p->d_ray, (void *)p->d_ray_rec,
                     (void *)p->d_nsamp, (void *)p->d_taps, (void *)p->d_chan_s,
                     (void *)p->d_tc_hi, (void *)p->d_tc_lo, (void *)p->d_err,
                     (void *)p->d_parker, (void *)p->d_cosw, (void *)p->d_view_z,
@@ -407,13 +412,18 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
         if (!(r < R))
             for (float &c : p->gather_atan_coef) c = 0.0f;
     }
-    std::vector<float> ray_inv(t.ray.size() / 2);
-    for (size_t r = 0; r < ray_inv.size() / 2; ++r)
+    // the adjoint gather's 32-byte ray records (one load per candidate ray)
+    std::vector<float> ray_rec(t.ray.size() * 2);
+    for (size_t r = 0; r < t.ray.size() / 4; ++r) {
+        for (int k = 0; k < 4; ++k) ray_rec[8 * r + k] = t.ray[4 * r + k];
         for (int k = 0; k < 2; ++k) {
             const float st = t.ray[4 * r + 2 + k];
             // a zero step gets 1e30: the adjoint's support bounds become +-inf-like
-            ray_inv[2 * r + k] = st != 0.0f ? (float)(1.0 / (double)st) : 1e30f;
+            ray_rec[8 * r + 4 + k] = st != 0.0f ? (float)(1.0 / (double)st) : 1e30f;
         }
+        std::memcpy(&ray_rec[8 * r + 6], &t.nsamp[r], sizeof(float));
+        ray_rec[8 * r + 7] = 0.0f;
+    }
     p->n_rows = n_rows;
     p->nz = nz;
     p->view_z_min = p->view_z_max = 0.0f;
@@ -435,7 +445,7 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
         (st = upload(p, &p->d_col_tan, t.col_tan)) != CT_OK ||
         (st = upload(p, &p->d_ray, t.ray)) != CT_OK ||
         (st = upload(p, &p->d_nsamp, t.nsamp)) != CT_OK ||
-        (st = upload(p, &p->d_ray_inv, ray_inv)) != CT_OK ||
+        (st = upload(p, &p->d_ray_rec, ray_rec)) != CT_OK ||
         (st = upload(p, &p->d_taps, t.taps)) != CT_OK ||
         (st = upload(p, &p->d_chan_s, t.chan_s)) != CT_OK ||
         (st = upload(p, &p->d_parker, t.parker)) != CT_OK ||

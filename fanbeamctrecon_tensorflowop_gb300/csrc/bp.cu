@@ -30,10 +30,34 @@ constexpr int kTile = kBpTile;
 constexpr int kBptSlices = 4;
 constexpr int kRowsPerThr = kBpRowsPerThr;
 
-// PAIRS: slice group z reads tap image z of `pairs` ([V][C+1] x SB/2 float4
-// each); ROWS pixels per thread (tiles of 32 x 8 ROWS)
+// PAIRS: slice group z reads the SB/4 four-slice tap planes SB/4 z ..
+// ([V][C+1] x 2 float4 each); ROWS pixels per thread (tiles of 32 x 8 ROWS).
+// Resident blocks per SM of the tap-image forms, measured for 32 clinical
+// slices (all forms give the same bits):
+//   four slices per thread: BP (2 rows) 3.42 / 3.21 ms with 6 / 5 blocks,
+//     the weighted form (1 row) 3.78 / 4.62 ms;
+//   eight slices per thread: BP (2 rows) 2.89 ms with 4 blocks; BP at 1 row
+//     2.98 ms with 4; the weighted form (1 row) 3.71 / 4.53 / 4.03 ms with
+//     4 / 5 / 6 blocks (5 and 6 spill).
+#ifndef CT_BP4_MINB1
+#define CT_BP4_MINB1 6
+#endif
+#ifndef CT_BP4_MINB2
+#define CT_BP4_MINB2 5
+#endif
+#ifndef CT_BP8_MINB1
+#define CT_BP8_MINB1 4
+#endif
+#ifndef CT_BP8_MINB2
+#define CT_BP8_MINB2 4
+#endif
+constexpr int bp_min_blocks(bool pairs, int sb, int rows) {
+    return !pairs || rows > 2 ? 1
+           : sb == 8          ? (rows == 1 ? CT_BP8_MINB1 : CT_BP8_MINB2)
+                              : (rows == 1 ? CT_BP4_MINB1 : CT_BP4_MINB2);
+}
 template <bool WEIGHTED, int SB, int DEG, bool TEX, bool PAIRS, int ROWS = kBpRowsPerThr>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, bp_min_blocks(PAIRS, SB, ROWS))
     bp_fan_kernel(const float *__restrict__ sino, const float4 *__restrict__ pairs,
                   float *__restrict__ img, const float2 *__restrict__ view_cs, BpArgs a,
                   int batch) {
@@ -49,7 +73,9 @@ __global__ void __launch_bounds__(256)
 
 // Tap images of slice groups of SB: group z, view v, column position i in
 // [0, C]: the taps (i0, i1) = (max(i-1, 0), min(i, C-1)) of slices
-// SB z .. SB z + SB-1 (zero past `batch`), as SB/2 float4.
+// SB z .. SB z + SB-1 (zero past `batch`), as SB/2 float4; float4 h holds
+// slices (2h, 2h+1) as (i0 of both, i1 of both), the f32x2 operands of the
+// backprojector's paired interpolation.
 template <int SB>
 __global__ void __launch_bounds__(256)
     bp_pairs_kernel(const float *__restrict__ sino, float4 *__restrict__ pairs, int V, int C,
@@ -65,8 +91,8 @@ __global__ void __launch_bounds__(256)
         for (int s = 0; s < 2; ++s) {
             const int b = SB * z + 2 * h + s;
             const float *row = sino + ((size_t)b * V + v) * C;
-            t[2 * s] = b < batch ? __ldg(row + i0) : 0.0f;
-            t[2 * s + 1] = b < batch ? __ldg(row + i1) : 0.0f;
+            t[s] = b < batch ? __ldg(row + i0) : 0.0f;
+            t[2 + s] = b < batch ? __ldg(row + i1) : 0.0f;
         }
         q[h] = make_float4(t[0], t[1], t[2], t[3]);
     }
@@ -241,6 +267,15 @@ void launch_bpt_any(bool w, bool tex, int deg, dim3 grid, cudaStream_t s, const 
 // eight with 2 pixel rows per thread, the same accumulators per thread,
 // measured 5.25 ms for 32 clinical slices against 4.08 ms.)
 constexpr int kPairSlices = 64;
+#ifndef CT_BP_SB8
+#define CT_BP_SB8 1
+#endif
+#ifndef CT_BP8_ROWS
+#define CT_BP8_ROWS 2
+#endif
+#ifndef CT_BP8_ROWS_W
+#define CT_BP8_ROWS_W 1
+#endif
 
 int pair_group(int batch) { return batch >= 4 ? 4 : 0; }
 
@@ -271,19 +306,46 @@ int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weigh
             float *ip = img + (size_t)b0 * plane;
             bp_pairs_kernel<4><<<dim3((a.C + 1 + 255) / 256, a.V, groups), 256, 0, s>>>(
                 sp, pairs, a.V, a.C, nb);
-            // pixel rows per thread (tiles of 32 x 8 rows): 2 for BP, 1 for the
-            // weighted form (32 clinical slices: BP 4.10 / 3.64 / 3.73 ms with 4 / 2 / 1
-            // rows, FBP 4.94 / 4.29 / 4.21 ms); fewer rows, fewer registers, more blocks
-            if (weighted) {
-                dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 7) / 8, groups);
-                launch_bp_any<4, true, 1>(true, tex, p->atan_deg, grid, s, sp, pairs, ip, vcs,
-                                          a, nb);
-            } else {
-                dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 15) / 16, groups);
-                launch_bp_any<4, true, 2>(false, tex, p->atan_deg, grid, s, sp, pairs, ip, vcs,
-                                          a, nb);
+            ct_count_launch();
+            // Groups of eight slices read two four-slice planes per pixel-view and
+            // share its geometry over eight slices; the rest take groups of four
+            // (32 clinical slices: BP 3.21 -> 2.89 ms, FBP 3.78 -> 3.71 ms).
+            // Pixel rows per thread (tiles of 32 x 8 rows): fewer rows, fewer
+            // registers, more blocks (four slices per thread, before the f32x2
+            // pairs: BP 4.10 / 3.64 / 3.73 ms with 4 / 2 / 1 rows, FBP 4.94 / 4.29 /
+            // 4.21 ms).
+            const int n8 = CT_BP_SB8 ? nb / 8 * 8 : 0;
+            const size_t plane4 = (size_t)a.V * (a.C + 1) * 2;  // float4 per tap plane
+            if (n8) {
+                if (weighted) {
+                    dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 8 * CT_BP8_ROWS_W - 1) /
+                                                              (8 * CT_BP8_ROWS_W), n8 / 8);
+                    launch_bp_any<8, true, CT_BP8_ROWS_W>(true, tex, p->atan_deg, grid, s, sp,
+                                                          pairs, ip, vcs, a, n8);
+                } else {
+                    dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 8 * CT_BP8_ROWS - 1) /
+                                                              (8 * CT_BP8_ROWS), n8 / 8);
+                    launch_bp_any<8, true, CT_BP8_ROWS>(false, tex, p->atan_deg, grid, s, sp,
+                                                        pairs, ip, vcs, a, n8);
+                }
+                ct_count_launch();
             }
-            ct_count_launch(2);
+            if (nb > n8) {
+                const int g4 = (nb - n8 + 3) / 4;
+                const float *sp4 = sp + (size_t)n8 * slice;
+                const float4 *pairs4 = pairs + (size_t)(n8 / 4) * plane4;
+                float *ip4 = ip + (size_t)n8 * plane;
+                if (weighted) {
+                    dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 7) / 8, g4);
+                    launch_bp_any<4, true, 1>(true, tex, p->atan_deg, grid, s, sp4, pairs4, ip4,
+                                              vcs, a, nb - n8);
+                } else {
+                    dim3 grid((a.nx + kTile - 1) / kTile, (a.ny + 15) / 16, g4);
+                    launch_bp_any<4, true, 2>(false, tex, p->atan_deg, grid, s, sp4, pairs4,
+                                              ip4, vcs, a, nb - n8);
+                }
+                ct_count_launch();
+            }
         }
         return (int)cudaGetLastError();
     }

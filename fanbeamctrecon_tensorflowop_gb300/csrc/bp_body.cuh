@@ -56,11 +56,13 @@ __device__ __forceinline__ float tex_weight(float f) {
 // sino + s * sstride ([V][C]), image slice s at img + s * istride ([ny][nx]).
 // Block of 32 x 8 threads, ROWS pixels per thread (32 x 32 tiles by default);
 // block-uniform call.  TEX: texture-unit weights (tex_weight) instead of
-// exact FP32 ones.  PAIRS (SB = 4 or 8): the taps come from the slice group's
-// tap image `pairs` ([V][C+1] x SB/2 float4, 32-byte aligned: for column
-// position i, the clamped taps (i0, i1) of slices 0..SB-1), SB/4 32-byte
-// loads per pixel-view instead of 2 SB 4-byte gathers; same values, same
-// arithmetic.
+// exact FP32 ones.  PAIRS (SB = 4 or 8): the taps come from SB/4 consecutive
+// four-slice tap planes at `pairs` ([V][C+1] x 2 float4 each, 32-byte
+// aligned: for column position i, the clamped taps (i0, i1) of four slices,
+// float4 h holding (i0, i1) of slices (2h, 2h+1) as (i0, i0, i1, i1)), SB/4
+// 32-byte loads per pixel-view instead of 2 SB 4-byte gathers, and the
+// interpolation and accumulation of two slices per f32x2 instruction; same
+// values, same per-slice operations, so the same bits.
 template <bool WEIGHTED, int SB, int DEG, typename OutT, int ROWS = kBpRowsPerThr,
           bool TEX = false, bool PAIRS = false>
 __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t sstride,
@@ -85,10 +87,16 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
         any |= in[k];
     }
     float acc[SB][ROWS];
+    // PAIRS: slices (2j, 2j+1) as one f32x2 accumulator
+    unsigned long long acc2[PAIRS ? SB / 2 : 1][ROWS];
 #pragma unroll
     for (int s = 0; s < SB; ++s)
 #pragma unroll
         for (int k = 0; k < ROWS; ++k) acc[s][k] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < (PAIRS ? SB / 2 : 1); ++j)
+#pragma unroll
+        for (int k = 0; k < ROWS; ++k) acc2[j][k] = 0ull;
     if (__syncthreads_or(any)) {
         const float *sb[SB];
 #pragma unroll
@@ -111,32 +119,39 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
                     const int i0 = max(i - 1, 0), i1 = min(i, a.C - 1);
                     float wgt = 1.0f;
                     if (WEIGHTED) wgt = __fdividef(1.0f, fmaf(U, U, t * t));
-                    float v0[SB], v1[SB];
                     if constexpr (PAIRS) {
-                        // one 32-byte load per four slices (the entries are 32-byte aligned)
-                        const float4 *q = pairs + ((size_t)v * (a.C + 1) + i) * (SB / 2);
+                        // one 32-byte load per four slices (the entries are 32-byte
+                        // aligned); per slice pair the scalar path's operations as
+                        // f32x2 instructions (each lane rounds as the FP32 one)
+                        const float4 *q = pairs + ((size_t)v * (a.C + 1) + i) * 2;
+                        const size_t plane4 = (size_t)a.V * (a.C + 1) * 2;
                         const bool ok = (unsigned)i <= (unsigned)a.C;
+                        const unsigned long long ff = pack2(f, f), ww = pack2(wgt, wgt);
 #pragma unroll
                         for (int h = 0; h < SB / 4; ++h) {
                             float4 t, u;
-                            ldg_v8(ok, q + 2 * h, t, u);
-                            v0[4 * h] = t.x, v1[4 * h] = t.y, v0[4 * h + 1] = t.z,
-                                     v1[4 * h + 1] = t.w;
-                            v0[4 * h + 2] = u.x, v1[4 * h + 2] = u.y, v0[4 * h + 3] = u.z,
-                                         v1[4 * h + 3] = u.w;
+                            ldg_v8(ok, q + h * plane4, t, u);
+                            const unsigned long long a0 = pack2(t.x, t.y), a1 = pack2(t.z, t.w);
+                            const unsigned long long b0 = pack2(u.x, u.y), b1 = pack2(u.z, u.w);
+                            const unsigned long long va = fma2(ff, sub2(a1, a0), a0);
+                            const unsigned long long vb = fma2(ff, sub2(b1, b0), b0);
+                            unsigned long long &ca = acc2[2 * h][k], &cb = acc2[2 * h + 1][k];
+                            ca = WEIGHTED ? fma2(va, ww, ca) : add2(ca, va);
+                            cb = WEIGHTED ? fma2(vb, ww, cb) : add2(cb, vb);
                         }
                     } else {
+                        float v0[SB], v1[SB];
                         const bool ok = (unsigned)i0 < (unsigned)a.C && (unsigned)i1 < (unsigned)a.C;
 #pragma unroll
                         for (int s = 0; s < SB; ++s) {
                             v0[s] = CT_DLOAD(ok, sb[s] + ro + i0);
                             v1[s] = CT_DLOAD(ok, sb[s] + ro + i1);
                         }
-                    }
 #pragma unroll
-                    for (int s = 0; s < SB; ++s) {
-                        const float val = fmaf(f, v1[s] - v0[s], v0[s]);
-                        acc[s][k] = WEIGHTED ? fmaf(val, wgt, acc[s][k]) : acc[s][k] + val;
+                        for (int s = 0; s < SB; ++s) {
+                            const float val = fmaf(f, v1[s] - v0[s], v0[s]);
+                            acc[s][k] = WEIGHTED ? fmaf(val, wgt, acc[s][k]) : acc[s][k] + val;
+                        }
                     }
                 }
             }
@@ -149,7 +164,12 @@ __device__ __forceinline__ void bp_tile(const float *__restrict__ sino, size_t s
 #pragma unroll
         for (int k = 0; k < ROWS; ++k) {
             const int iy = iy0 + 8 * k;
-            if (ix < a.nx && iy < a.ny) store_val(ib + (size_t)iy * a.nx + ix, acc[s][k]);
+            float r = acc[s][k];
+            if constexpr (PAIRS) {
+                const float2 pr = unpack2(acc2[s / 2][k]);
+                r = (s & 1) ? pr.y : pr.x;
+            }
+            if (ix < a.nx && iy < a.ny) store_val(ib + (size_t)iy * a.nx + ix, r);
         }
     }
 }

@@ -119,8 +119,8 @@ __global__ void __launch_bounds__(256)
 template <int SB, int DEG>
 __global__ void __launch_bounds__(kGThreads, adj_min_blocks(SB))
     fp_adjoint_cells_kernel(const float *__restrict__ sino, float *__restrict__ corners,
-                            const float4 *__restrict__ ray, const float2 *__restrict__ ray_inv,
-                            const int *__restrict__ nsamp, const float2 *__restrict__ view_cs,
+                            const float4 *__restrict__ ray_rec,
+                            const float2 *__restrict__ view_cs,
                             CellArgs a, int batch) {
     const int NXC = a.nx + 1, NYC = a.ny + 1;
     // block = 16 x 16 cells; a warp takes a 4 x 8 patch, whose cells see more
@@ -179,10 +179,11 @@ __global__ void __launch_bounds__(kGThreads, adj_min_blocks(SB))
             const int c0 = max(0, (int)ceilf(fmaxf(clo, -1.0f)));
             const int c1 = min(a.C - 1, (int)floorf(fminf(chi, (float)a.C)));
             for (int c = c0; c <= c1; ++c) {
-                const int n = __ldg(nsamp + row + c);
+                // the ray's 32-byte record: start and step (q), 1/step, count
+                float4 q, iv;
+                ldg_v8((unsigned)c < (unsigned)a.C, ray_rec + 2 * (row + c), q, iv);
+                const int n = __float_as_int(iv.z);
                 if (n <= 0) continue;
-                const float4 q = __ldg(ray + row + c);
-                const float2 iv = __ldg(ray_inv + row + c);
                 // samples with lo <= x0 + k s < hi; both neighbours of a cell
                 // boundary use the same threshold, so every sample lands in
                 // exactly one cell (a zero step has iv = 1e30: all or none)
@@ -304,8 +305,7 @@ int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, v
     for (int k = 0; k < 9; ++k) a.coef[k] = p->gather_atan_coef[k];
     const int deg = p->gather_atan_deg;
     const float2 *vcs = reinterpret_cast<const float2 *>(p->d_view_cs);
-    const float4 *ray = reinterpret_cast<const float4 *>(p->d_ray);
-    const float2 *rinv = reinterpret_cast<const float2 *>(p->d_ray_inv);
+    const float4 *rrec = reinterpret_cast<const float4 *>(p->d_ray_rec);
     cudaStream_t s = (cudaStream_t)stream;
     const size_t plane = (size_t)a.nx * a.ny, slice = (size_t)a.V * a.C;
     const int chunk = batch < 64 ? batch : 64;
@@ -328,7 +328,7 @@ int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, v
             interleave_kernel<4><<<ib, 256, 0, s>>>(sp, inter, nb, slice);
         dim3 grid((a.nx + kCellTile) / kCellTile, (a.ny + kCellTile) / kCellTile, groups);
         auto go = [&](auto kern) {
-            kern<<<grid, dim3(32, 8), 0, s>>>(inter, corners, ray, rinv, p->d_nsamp, vcs, a, nb);
+            kern<<<grid, dim3(32, 8), 0, s>>>(inter, corners, rrec, vcs, a, nb);
         };
         if (CT_ADJ_MAX_SB >= 16 && SB == 16)
             deg == 8 ? go(fp_adjoint_cells_kernel<16, 8>)

@@ -92,7 +92,9 @@ struct ct_plan {
     float *d_view_cs_lo;             // [2V] float-float remainder of d_view_cs
     float *d_col_tan;                // [2(C+1)] tan of the column boundaries (hi, lo)
     float *d_ray;                    // [4VC]
-    float *d_ray_inv;                // [2VC] 1/step (1e30 for a zero step), adjoint gather
+    float *d_ray_rec;                // [8VC] per ray, for the adjoint gather: start (x, y),
+                                     // step (x, y), 1/step (1e30 for a zero step), sample
+                                     // count (int32 bits), 0 (one 32-byte record)
     int32_t *d_nsamp;                // [VC]
     float *d_taps;                   // [2C-1]
     float *d_chan_s;                 // [2C]

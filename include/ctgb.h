@@ -177,8 +177,11 @@ uint32_t ct_build_flags(void);
  * instead malloc'ed and freed its buffers inside every call and exited the
  * process when one failed (FP/transform.cu:198-217, checkCudaErrors).
  *   alloc(ctx, bytes, stream): device memory for work that will be enqueued
- *     on `stream` (NULL for plan tables); NULL on failure, which the call
- *     reports as CT_ERR_ALLOC after releasing what it already took.
+ *     on `stream` (NULL for plan tables), 256-byte aligned as cudaMalloc's
+ *     (kernels read plan tables with 32-byte loads); NULL on failure, which
+ *     the call reports as CT_ERR_ALLOC after releasing what it already took.
+ *     A block that is not 256-byte aligned is given back and reported the
+ *     same way.
  *   free(ctx, ptr, stream): ptr is no longer needed once the work already
  *     enqueued on `stream` has run (stream-ordered, as cudaFreeAsync); for
  *     plan tables stream is NULL and the plan's work must have finished. */
