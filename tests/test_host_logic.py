@@ -92,3 +92,54 @@ def test_gloo_two_ranks_shard_and_reduce():
     for rank, owned, t in res:
         assert owned == [1] * batch
         assert t == 1.0  # max over ranks of (rank+1)/2
+
+
+def _worker_op(rank, world, port, batch, q):
+    """Each rank projects its own shard of a seeded batch (the FP64 oracle
+    stands in for the operator: no GPU here) and the shards are gathered in
+    rank order, as the replicas of a multi-GPU run split a batch."""
+    import torch
+    import torch.distributed as dist
+    import oracle
+    from fanbeamctrecon_tensorflowop_gb300.geometry import angle as _angle
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    oracle.build()
+    p = fan_param16(sdd=949.0, sid=541.0, n_views=16, n_cols=40, n=24, pixel_mm=4.0,
+                    dcol_rad=4.0 / 949.0)
+    ang = _angle(16, 0.0)
+    g = oracle.decode(p)
+    imgs = np.random.default_rng(5).random((batch, 24, 24), dtype=np.float32)
+    a, b = shard_range(batch, rank, world)
+    mine = oracle.fp_fan(g, ang, imgs[a:b]) if b > a else np.zeros((0, 16, 40))
+    # pad to the largest shard so every rank sends the same shape
+    rows = shard_range(batch, 0, world)[1]
+    buf = torch.zeros((rows, 16, 40), dtype=torch.float64)
+    buf[: b - a] = torch.from_numpy(np.asarray(mine, np.float64))
+    parts = [torch.zeros_like(buf) for _ in range(world)]
+    dist.all_gather(parts, buf)
+    if rank == 0:
+        got = np.concatenate([parts[r][: shard_range(batch, r, world)[1]
+                                        - shard_range(batch, r, world)[0]].numpy()
+                              for r in range(world)])
+        want = np.asarray(oracle.fp_fan(g, ang, imgs), np.float64)
+        q.put((got.shape == want.shape, bool(np.array_equal(got, want))))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_gloo_two_ranks_run_their_shards():
+    world, batch = 2, 5
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker_op, args=(r, world, port, batch, q))
+             for r in range(world)]
+    for p in procs:
+        p.start()
+    same_shape, equal = q.get(timeout=180)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert same_shape and equal
