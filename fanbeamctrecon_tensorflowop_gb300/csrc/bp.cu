@@ -36,9 +36,9 @@ constexpr int kRowsPerThr = kBpRowsPerThr;
 // slices (all forms give the same bits):
 //   four slices per thread: BP (2 rows) 3.42 / 3.21 ms with 6 / 5 blocks,
 //     the weighted form (1 row) 3.78 / 4.62 ms;
-//   eight slices per thread: BP (2 rows) 2.89 ms with 4 blocks; BP at 1 row
-//     2.98 ms with 4; the weighted form (1 row) 3.71 / 4.53 / 4.03 ms with
-//     4 / 5 / 6 blocks (5 and 6 spill).
+//   eight slices per thread: BP (2 rows) 2.89 / 2.99 ms with 4 / 3 blocks; BP
+//     at 1 row 2.98 ms with 4; the weighted form at 2 rows 3.50 ms with 4
+//     blocks, at 1 row 3.71 / 4.53 / 4.03 ms with 4 / 5 / 6 (5 and 6 spill).
 #ifndef CT_BP4_MINB1
 #define CT_BP4_MINB1 6
 #endif
@@ -274,7 +274,7 @@ constexpr int kPairSlices = 64;
 #define CT_BP8_ROWS 2
 #endif
 #ifndef CT_BP8_ROWS_W
-#define CT_BP8_ROWS_W 1
+#define CT_BP8_ROWS_W 2
 #endif
 
 int pair_group(int batch) { return batch >= 4 ? 4 : 0; }
@@ -309,7 +309,7 @@ int bp_fan(const ct_plan *p, const float *sino, float *img, int batch, int weigh
             ct_count_launch();
             // Groups of eight slices read two four-slice planes per pixel-view and
             // share its geometry over eight slices; the rest take groups of four
-            // (32 clinical slices: BP 3.21 -> 2.89 ms, FBP 3.78 -> 3.71 ms).
+            // (32 clinical slices: BP 3.21 -> 2.89 ms, FBP 3.78 -> 3.50 ms).
             // Pixel rows per thread (tiles of 32 x 8 rows): fewer rows, fewer
             // registers, more blocks (four slices per thread, before the f32x2
             // pairs: BP 4.10 / 3.64 / 3.73 ms with 4 / 2 / 1 rows, FBP 4.94 / 4.29 /
