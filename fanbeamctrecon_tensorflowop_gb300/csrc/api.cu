@@ -193,7 +193,8 @@ void free_plan(ct_plan *p) {
     if (!p) return;
     for (void *t : {(void *)p->d_view_cs, (void *)p->d_view_cs_lo, (void *)p->d_col_tan,
                     (void *)p->d_ray, (void *)p->d_ray_rec,
-                    (void *)p->d_nsamp, (void *)p->d_taps, (void *)p->d_chan_s,
+                    (void *)p->d_nsamp, (void *)p->d_fp_order, (void *)p->d_taps,
+                    (void *)p->d_chan_s,
                     (void *)p->d_tc_hi, (void *)p->d_tc_lo, (void *)p->d_err,
                     (void *)p->d_parker, (void *)p->d_cosw, (void *)p->d_view_z,
                     (void *)p->d_bpt_warp, (void *)p->d_bpt_bnd, (void *)p->d_bpt_ray,
@@ -445,6 +446,9 @@ static ct_status plan_create(const ct_fan_geom *geom, int n_rows, int nz, bool c
         (st = upload(p, &p->d_col_tan, t.col_tan)) != CT_OK ||
         (st = upload(p, &p->d_ray, t.ray)) != CT_OK ||
         (st = upload(p, &p->d_nsamp, t.nsamp)) != CT_OK ||
+        (st = upload(p, &p->d_fp_order,
+                     ctk::fp_block_order(geom->n_views, geom->n_cols, t.ray, t.nsamp))) !=
+            CT_OK ||
         (st = upload(p, &p->d_ray_rec, ray_rec)) != CT_OK ||
         (st = upload(p, &p->d_taps, t.taps)) != CT_OK ||
         (st = upload(p, &p->d_chan_s, t.chan_s)) != CT_OK ||

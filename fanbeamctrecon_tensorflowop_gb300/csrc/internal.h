@@ -96,6 +96,8 @@ struct ct_plan {
                                      // step (x, y), 1/step (1e30 for a zero step), sample
                                      // count (int32 bits), 0 (one 32-byte record)
     int32_t *d_nsamp;                // [VC]
+    int32_t *d_fp_order;             // launch order of the forward projector's blocks
+                                     // (fp_block_order)
     float *d_taps;                   // [2C-1]
     float *d_chan_s;                 // [2C]
     float *d_tc_hi, *d_tc_lo;        // tensor-core filter: TF32 split of the Toeplitz taps
@@ -117,6 +119,11 @@ namespace ctk {
 int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *work,
            void *stream);
 size_t fp_fan_work_bytes(const ct_plan *p, int batch);
+// The forward projector's block order (host, at plan creation): its blocks
+// (32 channels x 4 adjacent views) sorted by the quad layout most of their
+// rays walk, channel-group-major within a layout.
+std::vector<int32_t> fp_block_order(int V, int C, const std::vector<float> &ray,
+                                    const std::vector<int32_t> &nsamp);
 // work: fp_fan_adjoint_work_bytes(p, batch) bytes (corner sums of up to 64 slices)
 size_t fp_fan_adjoint_work_bytes(const ct_plan *p, int batch);
 int fp_fan_adjoint(const ct_plan *p, const float *sino, float *img, int batch, void *work,
