@@ -11,14 +11,15 @@
 //
 // Tiles of 128 rows x 224 columns, K steps of 16 FP32 (64-byte swizzled
 // rows): per step TMA brings the input tile (8 KB) and the two tap tiles
-// (14 KB each), two warps split the input tile, and one thread issues 2
+// (14 KB each), three warps split the input tile, and one thread issues 2
 // K-slices x 3 tcgen05.mma (M=128, N=224, K=8, kind::tf32).  A ring of four
 // such stages (176 KB) lets the copies and the split of later steps run while
 // the tensor core works.  Measured per 32 clinical slices (31,488 rows of 888
 // channels, CUDA events): one single-stage step at a time 0.389 ms; two
 // stages of K 32 0.282 ms; persistent with a double-buffered accumulator
 // 0.275 ms; four stages of K 16 0.244 ms (three 0.287, five 0.251; tiles of
-// 128 / 96 / 64 columns 0.33 .. 0.53 ms).  All forms give identical bits.
+// 128 / 96 / 64 columns 0.33 .. 0.53 ms); three splitter warps instead of two
+// 0.233 ms.  All forms give identical bits.
 #include <cuda.h>
 
 #include <cstring>
@@ -131,12 +132,18 @@ __device__ __forceinline__ float tf32_hi(float x) {
 //     have completed, tracked by tcgen05.commit on empty[s]);
 //   1, one lane: MMA issuer (waits for the stage's split, and for the
 //     epilogue to have drained the accumulator it reuses);
-//   2-3: split the input tile in place (A -> A_hi) and into A_lo;
-//   4-7: epilogue (warp 4+q reads accumulator lanes 32q..32q+31).
+//   2 .. 1+TC_SPLIT: split the input tile in place (A -> A_hi) and into A_lo;
+//   the last four: epilogue (warp w reads accumulator lanes 32 (w mod 4) ..,
+//     the lanes tcgen05.ld gives a warp).
 // Every wait is bounded; on a timeout the roles stop issuing, the MMA lane
 // still commits what it issued, the producer waits (bounded) for copies in
 // flight, the plan's error flag is raised and the tensor memory is freed.
-constexpr int TC3_THREADS = 256;
+// Splitter warps (32 clinical slices: 2 / 3 / 4 warps 0.244 / 0.233 / 0.237 ms).
+#ifndef CT_TC_SPLIT
+#define CT_TC_SPLIT 3
+#endif
+constexpr int TC_SPLIT = CT_TC_SPLIT;
+constexpr int TC3_THREADS = 32 * (2 + TC_SPLIT + 4);
 
 __global__ void __launch_bounds__(TC3_THREADS)
     ramp_tc_kernel(const __grid_constant__ CUtensorMap map_in,
@@ -162,7 +169,7 @@ __global__ void __launch_bounds__(TC3_THREADS)
     if (tid == 0) {
         for (int s = 0; s < TC2_STAGES; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&split[s], 2);
+            mbar_init(&split[s], TC_SPLIT);
             mbar_init(&empty[s], 1);
         }
         for (int a = 0; a < 2; ++a) {
@@ -245,8 +252,8 @@ __global__ void __launch_bounds__(TC3_THREADS)
             // completes once every MMA issued above has
             mma_commit(done);
         }
-    } else if (warp < 4) {
-        // splitters: 64 threads, each stage's 1024 float4 in place
+    } else if (warp < 2 + TC_SPLIT) {
+        // splitters: 32 TC_SPLIT threads, each stage's float4 in place
         const int t = tid - 64;
         int g = 0;
         for (int j = 0; j < my_tiles; ++j) {
@@ -261,7 +268,7 @@ __global__ void __launch_bounds__(TC3_THREADS)
                 float4 *a = reinterpret_cast<float4 *>(sA(s));
                 float4 *lo = reinterpret_cast<float4 *>(sAlo(s));
 #pragma unroll 4
-                for (int q = t; q < (int)(TC2_A_BYTES / 16); q += 64) {
+                for (int q = t; q < (int)(TC2_A_BYTES / 16); q += 32 * TC_SPLIT) {
                     const float4 x = a[q];
                     float4 h, l;
                     h.x = tf32_hi(x.x); l.x = x.x - h.x;
@@ -281,8 +288,8 @@ __global__ void __launch_bounds__(TC3_THREADS)
             if (stop) break;
         }
     } else {
-        // epilogue warps 4-7: accumulator lanes 32 (warp - 4) ..
-        const int q4 = warp - 4;
+        // epilogue warps: accumulator lanes 32 (warp mod 4) ..
+        const int q4 = warp & 3;
         for (int j = 0; j < my_tiles; ++j) {
             const int a = j & 1;
             const bool ok = mbar_wait(&acc_full[a], (j >> 1) & 1);
