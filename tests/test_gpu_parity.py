@@ -107,6 +107,24 @@ def test_bp_and_adjoint(case, cuda, orc):
         assert np.array_equal(got_t[1], _np(plan.bp_adjoint(_t(x[1:2], cuda)))[0])
 
 
+@pytest.mark.parametrize("nb", [4, 8, 13, 21])
+def test_bp_fbp_tap_image_groups(case, cuda, orc, nb):
+    """Batches of four or more read tap images: groups of eight slices per
+    thread, then groups of four for the rest (the last one ragged).  Every
+    slice equals the slice alone (one slice per thread, gathers) bit for bit,
+    and the BP meets the oracle."""
+    name, p, a, plan, plan_sl, g = case
+    y = _sinos(g, nb, seed=3)
+    yt = _t(y, cuda)
+    for op in (plan.bp, plan.fbp, plan_sl.fbp):
+        got = _np(op(yt))
+        for b in sorted({0, nb // 2, nb - 1}):
+            assert np.array_equal(got[b], _np(op(yt[b:b + 1]))[0]), (nb, b)
+    ref = orc.bp_fan(g, a, y)
+    got = _np(plan.bp(yt))
+    assert rel_l2(got, ref) <= TOL, rel_l2(got, ref)
+
+
 @pytest.mark.parametrize("nb", [16, 40])
 def test_transpose_slice_groups(case, cuda, orc, nb):
     """Batches of 16 and 40 slices through the BP / FBP transposes (four
