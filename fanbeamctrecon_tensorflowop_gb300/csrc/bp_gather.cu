@@ -59,12 +59,6 @@ __device__ __forceinline__ unsigned long long dup2(float x) { return pack2(x, x)
 #define CT_BPG_NQ 4
 #endif
 
-// Lines of the walk whose pixels one loop takes in turn.
-#ifndef CT_BPG_LINE_GROUP
-#define CT_BPG_LINE_GROUP 2
-#endif
-constexpr int kBpgLineGroup = CT_BPG_LINE_GROUP;
-
 // NQ quads = 4 NQ slices per launch slice group (blockIdx.y).
 template <bool WEIGHTED, int NQ>
 __global__ void __launch_bounds__(128, CT_BPG_MINB)
@@ -95,78 +89,57 @@ __global__ void __launch_bounds__(128, CT_BPG_MINB)
 
     long long Xl = bl.x, Xh = bh.x;
     const int lines = active ? J1 - J0 + 1 : 0;
-    const int nlines = colwalk ? a.nx : a.ny;
-    // line t of the walk: its strip pixels [i, i1], the lower boundary's
-    // crossing hl + F, Lb and the line's pixels; the crossings then step on
-    int t = 0, j = J0, i = 0, i1 = -1, hl = 0;
-    float F = 0.0f, Lb = 0.0f;
-    const float4 *line = img;
-    auto start_line = [&]() {
-        j = J0 + t;
-        hl = (int)(Xl >> 32);
-        const int hh = (int)(Xh >> 32);
+    for (int t = 0; t < lines; ++t) {
+        const int j = J0 + t;
+        const int hl = (int)(Xl >> 32), hh = (int)(Xh >> 32);
         const unsigned fl = (unsigned)Xl, fh = (unsigned)Xh;
         // the strip's pixels on this line: between the two crossings, the
         // lower boundary included (gamma_b <= gamma_p < gamma_{b+1})
+        int i0, i1;
         if (pos) {
-            i = hl + (fl != 0u);
+            i0 = hl + (fl != 0u);
             i1 = hh + (fh != 0u) - 1;
         } else {
-            i = hh + 1;
+            i0 = hh + 1;
             i1 = hl;
         }
         const int2 fr = __ldg(fov + j);
-        i = max(i, fr.x);
+        i0 = max(i0, fr.x);
         i1 = min(i1, fr.y);
-        F = __uint2float_rn(fl) * 2.3283064365386963e-10f;  // 2^-32
-        Lb = fmaf((float)t, rr.y, rr.x);
-        line = img + (size_t)j * npx;
+        if (i0 <= i1) {
+            const float F = __uint2float_rn(fl) * 2.3283064365386963e-10f;  // 2^-32
+            const float Lb = fmaf((float)t, rr.y, rr.x);
+            const float4 *line = img + (size_t)j * npx;
+            const int nlines = colwalk ? a.nx : a.ny;
+            for (int i = i0; i <= i1; ++i) {
+                const bool ok = (unsigned)i < (unsigned)npx && (unsigned)j < (unsigned)nlines;
+                const float dp = (float)(i - hl) - F;  // offset from the lower boundary (pixels)
+                const float n = dp * rr.z;              // normal distance (mm)
+                const float L = fmaf(dp, rr.w, Lb);     // distance along the boundary ray (mm)
+                const float q = __fdividef(n, L);
+                const float q2 = q * q;
+                // atan(q) for |q| <= dcol: q (1 - q^2/3 + q^4/5)
+                const float f = q * fmaf(q2, fmaf(q2, 0.2f, -0.33333334f), 1.0f) * a.inv_dcol;
+                float wa = 1.0f - f, wb = f;
+                if (WEIGHTED) {
+                    const float w = __fdividef(1.0f, fmaf(L, L, n * n));  // 1 / (U^2 + t^2)
+                    wa *= w;
+                    wb *= w;
+                }
+                const unsigned long long pa = dup2(wa), pb = dup2(wb);
+#pragma unroll
+                for (int h = 0; h < NQ; ++h) {
+                    const float4 x = CT_DLOAD(ok, line + h * qplane + i);
+                    const unsigned long long x01 = pack2(x.x, x.y), x23 = pack2(x.z, x.w);
+                    A[2 * h] = fma2(pa, x01, A[2 * h]);
+                    A[2 * h + 1] = fma2(pa, x23, A[2 * h + 1]);
+                    B[2 * h] = fma2(pb, x01, B[2 * h]);
+                    B[2 * h + 1] = fma2(pb, x23, B[2 * h + 1]);
+                }
+            }
+        }
         Xl += bl.y;
         Xh += bh.y;
-    };
-    // Lines in groups of kBpgLineGroup: one loop takes a lane's pixels of all
-    // of them (line by line, in order), so the warp iterates the maximum over
-    // its lanes of the group's pixel count, not the sum of the per-line
-    // maxima.  The pixels keep their order: the same sums.
-    for (int t0 = 0; t0 < lines; t0 += kBpgLineGroup) {
-        t = t0;
-        start_line();
-        int left = min(kBpgLineGroup, lines - t0) - 1;  // lines after t in this group
-        // bounded: at most npx pixels per line, and a step to each next line
-        for (int it = 0; it < kBpgLineGroup * (npx + 1); ++it) {
-            if (i > i1) {
-                if (left == 0) break;
-                --left;
-                ++t;
-                start_line();
-                continue;
-            }
-            const bool ok = (unsigned)i < (unsigned)npx && (unsigned)j < (unsigned)nlines;
-            const float dp = (float)(i - hl) - F;  // offset from the lower boundary (pixels)
-            const float n = dp * rr.z;              // normal distance (mm)
-            const float L = fmaf(dp, rr.w, Lb);     // distance along the boundary ray (mm)
-            const float q = __fdividef(n, L);
-            const float q2 = q * q;
-            // atan(q) for |q| <= dcol: q (1 - q^2/3 + q^4/5)
-            const float f = q * fmaf(q2, fmaf(q2, 0.2f, -0.33333334f), 1.0f) * a.inv_dcol;
-            float wa = 1.0f - f, wb = f;
-            if (WEIGHTED) {
-                const float w = __fdividef(1.0f, fmaf(L, L, n * n));  // 1 / (U^2 + t^2)
-                wa *= w;
-                wb *= w;
-            }
-            const unsigned long long pa = dup2(wa), pb = dup2(wb);
-#pragma unroll
-            for (int h = 0; h < NQ; ++h) {
-                const float4 x = CT_DLOAD(ok, line + h * qplane + i);
-                const unsigned long long x01 = pack2(x.x, x.y), x23 = pack2(x.z, x.w);
-                A[2 * h] = fma2(pa, x01, A[2 * h]);
-                A[2 * h + 1] = fma2(pa, x23, A[2 * h + 1]);
-                B[2 * h] = fma2(pb, x01, B[2 * h]);
-                B[2 * h + 1] = fma2(pb, x23, B[2 * h + 1]);
-            }
-            ++i;
-        }
     }
     // channel c = strip c's f sum + strip c+1's (1-f) sum (+ the clamped taps)
     const int c = strip;
