@@ -81,9 +81,12 @@ __device__ __forceinline__ float4 tex_weights2d(float A, float B) {
 // Slices per thread of cone_bp_kernel.  The row coordinate of slice k is
 // formed from the height of its group's first slice, group_z(k & ~(kZC-1)),
 // plus (k mod kZC) row steps; the transpose forms it the same way, so both
-// sample each slice at the same fp32 row coordinate.
+// sample each slice at the same fp32 row coordinate.  Measured per two
+// clinical volumes (CUDA events): 16 slices, 6 blocks per SM: FDK 33.3 ms,
+// FDK adjoint 58.9 ms; 8 slices, 7 blocks: 32.2 / 56.4 ms (6 blocks: 39.0 ms
+// FDK).
 #ifndef CT_CONE_ZC
-#define CT_CONE_ZC 16
+#define CT_CONE_ZC 8
 #endif
 constexpr int kZC = CT_CONE_ZC;
 __device__ __forceinline__ float group_z(const ConeArgs &a, int k0) {
@@ -101,11 +104,12 @@ __device__ __forceinline__ float group_z(const ConeArgs &a, int k0) {
 // four 4-byte gathers, the same four values, and the two column lerps (rows
 // r0 and r1) as one f32x2 pair: the same operations per lane as the scalar
 // form, so the same bits.
-// 6 blocks of 256 threads per SM (40 registers): with QUAD, 17.9 ms per
-// clinical FDK volume, where the compiler's own choice (74-80 registers)
-// took 32.4 ms and 5 blocks 21.0 ms
+// Resident blocks of 256 threads per SM.  With 16 slices per thread, 6 (40
+// registers) gave 17.9 ms per clinical FDK volume, where the compiler's own
+// choice (74-80 registers) took 32.4 ms and 5 blocks 21.0 ms; with 8 slices
+// per thread, 7 blocks (32 registers).
 #ifndef CT_CONE_BP_MINB
-#define CT_CONE_BP_MINB 6
+#define CT_CONE_BP_MINB 7
 #endif
 template <int ZC, int DEG, bool TEX, bool QUAD>
 __global__ void __launch_bounds__(kThreads, CT_CONE_BP_MINB)
