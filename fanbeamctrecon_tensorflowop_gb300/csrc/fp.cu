@@ -23,12 +23,12 @@ namespace {
 // A block is one 32-channel group of kFpViews adjacent views (their rays
 // cross nearly the same cells, so the block's warps share L1 lines), and
 // blocks run channel-group-major: the warps resident at any time cover a few
-// channel groups of every view.  The plan's order table (fp_block_order)
-// runs the blocks whose rays walk the transposed layout after the others, so
-// the resident warps read one layout's quad images at a time.  Against 8 channel groups of one view per
+// channel groups of every view.  Against 8 channel groups of one view per
 // 256-thread block, in view order: 11.04 -> 8.72 ms per 32 clinical slices
 // (2 views per block 8.74, 8 views 8.97, 16 views 9.27; 1 view, channel-major
-// alone 8.87).
+// alone 8.87).  The plan's order table (fp_block_order) then runs the blocks
+// whose rays walk the transposed layout after the others, so the resident
+// warps read one layout's quad images at a time (8.73 -> 8.56 ms).
 constexpr int kFpViews = 4;
 constexpr int kFpThreads = 32 * kFpViews;
 constexpr int kFpChunk = 64;  // slices per quad-workspace chunk
