@@ -39,16 +39,40 @@ constexpr int kFpChunk = 64;  // slices per quad-workspace chunk
 #define CT_FP_MAX_SB 16
 #endif
 
-// Builds both quad layouts of nz slices (grid.z = 2 * slices).
+// Builds both quad layouts of nz slices (grid: 32 x 32-quad tiles x slices).
+// A block stages the tile's 33 x 33 clamped texels in shared memory with
+// coalesced reads, then writes the tile's quads of layout 0 (rows of quads
+// along x) and of layout 1 (the transposed image, rows along y), both
+// coalesced; the values are build_quad's (fp_body.cuh).  The former
+// one-quad-per-thread form read the transposed layout's taps down image
+// columns: 0.147 ms per 32 clinical slices.
 __global__ void __launch_bounds__(256)
     build_quads_kernel(const float *__restrict__ img, float4 *__restrict__ quads, int nx, int ny) {
+    __shared__ float t[33][33];
     const int Q = nx + 1;
-    const int qi = blockIdx.x * 32 + threadIdx.x, qj = blockIdx.y * 8 + threadIdx.y;
-    if (qi >= Q || qj >= Q) return;
-    const int layout = blockIdx.z & 1, b = blockIdx.z >> 1;
-    build_quad(img + (size_t)b * nx * ny,
-               quads + ((size_t)b * 2 + layout) * Q * Q + (size_t)qj * Q + qi, nx, ny, layout,
-               qi, qj);
+    const int TX = blockIdx.x * 32, TY = blockIdx.y * 32, b = blockIdx.z;
+    const float *im = img + (size_t)b * nx * ny;
+    // texel (TX - 1 + xx, TY - 1 + yy), clamped to the image
+    for (int k = threadIdx.y * 32 + threadIdx.x; k < 33 * 33; k += 256) {
+        const int yy = k / 33, xx = k - yy * 33;
+        const int x = min(max(TX - 1 + xx, 0), nx - 1), y = min(max(TY - 1 + yy, 0), ny - 1);
+        t[yy][xx] = __ldg(im + (size_t)y * nx + x);
+    }
+    __syncthreads();
+    const int i = threadIdx.x;
+    float4 *q0 = quads + (size_t)b * 2 * Q * Q, *q1 = q0 + (size_t)Q * Q;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int j = threadIdx.y + 8 * r;
+        // layout 0: quad (TX + i, TY + j) = cell (TX - 1 + i, TY - 1 + j)
+        if (TX + i < Q && TY + j < Q)
+            q0[(size_t)(TY + j) * Q + TX + i] =
+                make_float4(t[j][i], t[j][i + 1], t[j + 1][i], t[j + 1][i + 1]);
+        // layout 1: quad (TY + i, TX + j) = cell (u, v) = (TY - 1 + i, TX - 1 + j), u along y
+        if (TY + i < Q && TX + j < Q)
+            q1[(size_t)(TX + j) * Q + TY + i] =
+                make_float4(t[i][j], t[i + 1][j], t[i][j + 1], t[i + 1][j + 1]);
+    }
 }
 
 template <int SB>
@@ -120,7 +144,7 @@ int fp_fan(const ct_plan *p, const float *img, float *sino, int batch, void *wor
     // chunks of at most kFpChunk slices share the quad workspace
     for (int c0 = 0; c0 < batch; c0 += kFpChunk) {
         const int nb = batch - c0 < kFpChunk ? batch - c0 : kFpChunk;
-        build_quads_kernel<<<dim3((Q + 31) / 32, (Q + 7) / 8, 2 * nb), dim3(32, 8), 0, s>>>(
+        build_quads_kernel<<<dim3((Q + 31) / 32, (Q + 31) / 32, nb), dim3(32, 8), 0, s>>>(
             img + (size_t)c0 * plane, quads, nx, ny);
         ct_count_launch();
         float *out = sino + (size_t)c0 * n_rays;
