@@ -99,8 +99,9 @@ def test_texture_mode_against_oracle_and_adjoints(cuda, texture_oracle):
 
 
 def test_texture_mode_transpose_slice_groups(cuda, texture_oracle):
-    """The BP transpose of 16 slices with the texture weights: two slices
-    against the emulating oracle, dot test."""
+    """BP and its transpose on 16 slices with the texture weights (the BP in
+    groups of eight slices from tap images): two slices of each against the
+    emulating oracle, dot test."""
     orc = texture_oracle
     p, a = G.small(n=50, ny=38, shift=1.5, views=72, cols=100)
     g = orc.decode(p)
@@ -110,6 +111,10 @@ def test_texture_mode_transpose_slice_groups(cuda, texture_oracle):
     got = _np(plan.bp_adjoint(_t(x, cuda)))
     e = rel_l2(got[[0, 15]], orc.bp_fan_transpose(g, a, x[[0, 15]]))
     assert e <= TOL, e
+    y16 = np.random.default_rng(9).uniform(0, 1, (16, g.n_views, g.n_cols)).astype(np.float32)
+    got = _np(plan.bp(_t(y16, cuda)))
+    e = rel_l2(got[[0, 15]], orc.bp_fan(g, a, y16[[0, 15]]))
+    assert e <= ADJ_TOL.get("bp", TOL), e
     rng = np.random.default_rng(5)
     xx = rng.standard_normal((16, g.ny, g.nx)).astype(np.float32)
     yy = rng.standard_normal((16, g.n_views, g.n_cols)).astype(np.float32)
